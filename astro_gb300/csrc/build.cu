@@ -1,0 +1,838 @@
+// Encode, bounding box, tree topology and per-layer aggregation kernels.
+//
+// Reference stages replaced here (Astro/Renderer.swift:505-533,714-755):
+//   generateMortonCodes + fillIndices (MortonCode.metal:26-52, Octree.metal:39-51)
+//   countUniqueMortonCodes per layer: markUniques, the scan, scatterUniques,
+//     copyLastScanToParentCount (Octree.metal:282-334)
+//   aggregateLeafNodes / aggregateNodes (Octree.metal:53-202)
+// The reference finds the runs of every layer with one sort + scan + scatter
+// per layer over all N entries. Here a single pass over the sorted keys finds
+// the node starts of all layers at once (topology_kernel), and one kernel
+// per layer aggregates mass and centre of mass.
+#include <algorithm>
+
+#include "build_kernels.cuh"
+#include "common.cuh"
+#include "internal.h"
+
+namespace astro {
+
+// ------------------------------------------------------------- encode ----
+
+// generateMortonCodes with the reference quantiser (u32)(p + 1e6): the
+// float-to-uint conversion saturates and rounds toward zero.
+__global__ void encode_ref_kernel(const float4* __restrict__ pos, uint64_t* __restrict__ codes,
+                                  uint32_t n_tree, uint32_t unused_bits, float offset) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_tree) return;
+    const float4 q = pos[i];
+    const uint32_t x = __float2uint_rz(__fadd_rn(q.x, offset));
+    const uint32_t y = __float2uint_rz(__fadd_rn(q.y, offset));
+    const uint32_t z = __float2uint_rz(__fadd_rn(q.z, offset));
+    codes[i] = interleave3(x, y, z) >> unused_bits;
+}
+
+__device__ __forceinline__ uint32_t quantise(float x, float lo, float scale) {
+    return min(__float2uint_rz(__fmul_rn(__fsub_rn(x, lo), scale)), kQuantMax);
+}
+
+// Bounding-box quantiser of the PHYSICAL preset, one block per chunk. In the
+// precision form the FP32 frame relative to the system origin is written
+// to pos here (x64 is the master copy).
+template <bool kPrec>
+__global__ __launch_bounds__(256) void encode_phys_kernel(const Chunk* __restrict__ chunks,
+                                                          const SysInfo* __restrict__ sys,
+                                                          float4* __restrict__ pos,
+                                                          const double* __restrict__ x64,
+                                                          uint64_t* __restrict__ codes, uint32_t n,
+                                                          uint32_t lbits) {
+    const Chunk c = chunks[blockIdx.x];
+    const SysInfo& s = sys[c.sys];
+    const float lox = s.lo[0], loy = s.lo[1], loz = s.lo[2], scale = s.scale;
+    const uint32_t unused_bits = 63u - 3u * lbits;
+    const uint64_t sys_bits = (uint64_t)c.sys << (3u * lbits);
+    double ox = 0, oy = 0, oz = 0;
+    if (kPrec) {
+        ox = s.origin[0];
+        oy = s.origin[1];
+        oz = s.origin[2];
+    }
+    for (uint32_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
+        float4 q = pos[i];
+        if (kPrec) {
+            q.x = __double2float_rn(__dsub_rn(x64[i], ox));
+            q.y = __double2float_rn(__dsub_rn(x64[(size_t)n + i], oy));
+            q.z = __double2float_rn(__dsub_rn(x64[2 * (size_t)n + i], oz));
+            pos[i] = q;
+        }
+        const uint32_t qx = quantise(q.x, lox, scale);
+        const uint32_t qy = quantise(q.y, loy, scale);
+        const uint32_t qz = quantise(q.z, loz, scale);
+        codes[i] = sys_bits | (interleave3(qx, qy, qz) >> unused_bits);
+    }
+}
+
+// ------------------------------------------------------- bounding box ----
+
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(kFullMask, v, o));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFullMask, v, o));
+    return v;
+}
+
+// Block-level min/max of six ordered keys followed by one atomic per value.
+template <typename U>
+__device__ __forceinline__ void block_bbox_commit(U lo[3], U hi[3], U* acc) {
+    __shared__ U s_red[8][6];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = warp_min(lo[a]);
+        hi[a] = warp_max(hi[a]);
+    }
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) {
+            s_red[warp][a] = lo[a];
+            s_red[warp][3 + a] = hi[a];
+        }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const uint32_t nw = blockDim.x >> 5;
+        U v = s_red[0][threadIdx.x];
+        for (uint32_t w = 1; w < nw; ++w)
+            v = threadIdx.x < 3 ? min(v, s_red[w][threadIdx.x]) : max(v, s_red[w][threadIdx.x]);
+        if (threadIdx.x < 3) atomicMin(acc + threadIdx.x, v);
+        else atomicMax(acc + threadIdx.x, v);
+    }
+}
+
+// Bounding box of the current positions, one block per chunk, accumulated
+// per system with one atomic per block and value.
+template <bool kPrec>
+__global__ __launch_bounds__(256) void bbox_kernel(const Chunk* __restrict__ chunks,
+                                                   const float4* __restrict__ pos,
+                                                   const double* __restrict__ x64, uint32_t n,
+                                                   uint32_t* __restrict__ bb32,
+                                                   unsigned long long* __restrict__ bb64) {
+    const Chunk c = chunks[blockIdx.x];
+    if (kPrec) {
+        unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+        for (uint32_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x)
+            for (int a = 0; a < 3; ++a) {
+                unsigned long long o = f64_to_ordered(x64[(size_t)a * n + i]);
+                lo[a] = min(lo[a], o);
+                hi[a] = max(hi[a], o);
+            }
+        block_bbox_commit(lo, hi, bb64 + 6ull * c.sys);
+    } else {
+        uint32_t lo[3] = {~0u, ~0u, ~0u}, hi[3] = {0, 0, 0};
+        for (uint32_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
+            const float4 q = pos[i];
+            const float v[3] = {q.x, q.y, q.z};
+            for (int a = 0; a < 3; ++a) {
+                uint32_t o = f32_to_ordered(v[a]);
+                lo[a] = min(lo[a], o);
+                hi[a] = max(hi[a], o);
+            }
+        }
+        block_bbox_commit(lo, hi, bb32 + 6ull * c.sys);
+    }
+}
+
+// Per-system quantiser and opening thresholds from the box accumulators,
+// which are then reset for the next accumulation.
+template <bool kPrec>
+__global__ void setup_kernel(SysInfo* __restrict__ sys, uint32_t nsys,
+                             uint32_t* __restrict__ bb32, unsigned long long* __restrict__ bb64,
+                             uint32_t lbits, float theta, uint32_t root_offset) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    SysInfo& info = sys[s];
+    float lo[3], hi[3];
+    if (kPrec) {
+        for (int a = 0; a < 3; ++a) {
+            const double l = ordered_to_f64(bb64[6ull * s + a]);
+            const double h = ordered_to_f64(bb64[6ull * s + 3 + a]);
+            const double o = __dmul_rn(__dadd_rn(l, h), 0.5);
+            info.origin[a] = o;
+            lo[a] = __double2float_rn(__dsub_rn(l, o));
+            hi[a] = __double2float_rn(__dsub_rn(h, o));
+            bb64[6ull * s + a] = ~0ull;
+            bb64[6ull * s + 3 + a] = 0ull;
+        }
+    } else {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = ordered_to_f32(bb32[6ull * s + a]);
+            hi[a] = ordered_to_f32(bb32[6ull * s + 3 + a]);
+            info.origin[a] = 0.0;
+            bb32[6ull * s + a] = ~0u;
+            bb32[6ull * s + 3 + a] = 0u;
+        }
+    }
+    float ext = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        info.lo[a] = lo[a];
+        ext = fmaxf(ext, __fsub_rn(hi[a], lo[a]));
+    }
+    if (!(ext > 0.0f) || !isfinite(ext)) ext = 1.0f;
+    info.ext = ext;
+    info.scale = __fdiv_rn(kQuantCells, ext);
+    info.root = root_offset + s;
+    for (uint32_t l = 0; l <= lbits; ++l) {
+        const float c = __fdiv_rn(__fmul_rn(ext, exp2_exact((int)l - (int)lbits)), theta);
+        info.crit2[l] = __fmul_rn(c, c);
+    }
+}
+
+// ------------------------------------------------------------ reorder ----
+
+// Permute the PHYSICAL state into the new Morton order (B <- A[perm]).
+template <bool kPrec>
+__global__ void reorder_kernel(const uint32_t* __restrict__ perm, const float4* __restrict__ pos_a,
+                               const float4* __restrict__ vel_a, const uint32_t* __restrict__ id_a,
+                               const double* __restrict__ x_a, float4* __restrict__ pos_b,
+                               float4* __restrict__ vel_b, uint32_t* __restrict__ id_b,
+                               double* __restrict__ x_b, uint32_t n) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t s = perm[j];
+    pos_b[j] = pos_a[s];
+    vel_b[j] = vel_a[s];
+    id_b[j] = id_a[s];
+    if (kPrec) {
+        x_b[j] = x_a[s];
+        x_b[(size_t)n + j] = x_a[(size_t)n + s];
+        x_b[2 * (size_t)n + j] = x_a[2 * (size_t)n + s];
+    }
+}
+
+// ----------------------------------------------------------- topology ----
+
+constexpr int kTopoThreads = 256;
+constexpr int kTopoWarps = kTopoThreads / 32;
+constexpr int kTopoItems = 8;
+constexpr int kTopoTile = kTopoThreads * kTopoItems;
+
+// One pass over the sorted keys finds the nodes of every layer. Position i
+// starts a node at layer l when its key differs from key i-1 above bit 3l,
+// i.e. for l <= lev(i) = floor(msb(k[i] ^ k[i-1]) / 3) (capped at lbits;
+// lev(0) = lbits). The index of that node inside its layer is the number of
+// starts before i, found per layer with warp ballots and a decoupled
+// look-back across tiles. Each start writes the node's first particle and,
+// above layer 0, its first child (the node starting at i one layer down).
+// This yields the runs of markUniques/scatterUniques (Octree.metal:282-318)
+// for all layers without re-sorting or re-scanning per layer.
+__global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_off[ASTRO_MAX_LAYERS];
+    __shared__ uint32_t s_wcnt[kTopoWarps][32];
+    __shared__ uint32_t s_prefix[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lbits = (int)a.lbits;
+    if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+    if (tid < ASTRO_MAX_LAYERS) s_off[tid] = a.offset[tid];
+    if (tid < 32)
+        for (int w = 0; w < kTopoWarps; ++w) s_wcnt[w][tid] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kTopoTile;
+    if (base >= a.n) return;
+    const uint64_t warp_base = base + (uint64_t)warp * 32 * kTopoItems;
+    const uint32_t lt = lanemask_lt();
+
+    uint64_t key[kTopoItems];
+    int lev[kTopoItems];
+    uint64_t carry = (warp_base > 0 && warp_base <= a.n) ? a.keys[warp_base - 1] : 0ull;
+#pragma unroll
+    for (int k = 0; k < kTopoItems; ++k) {
+        const uint64_t i = warp_base + 32ull * k + lane;
+        const bool valid = i < a.n;
+        key[k] = valid ? a.keys[i] : 0ull;
+        uint64_t prev = __shfl_up_sync(kFullMask, key[k], 1);
+        if (lane == 0) prev = carry;
+        carry = __shfl_sync(kFullMask, key[k], 31);
+        int lv = -1;
+        if (valid) {
+            if (i == 0) lv = lbits;
+            else if (key[k] != prev) lv = min(lbits, (63 - __clzll((long long)(key[k] ^ prev))) / 3);
+        }
+        lev[k] = lv;
+    }
+    // Starts per layer within this warp (lane l keeps layer l).
+    uint32_t my_cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kTopoItems; ++k)
+        for (int l = 0; l <= lbits; ++l) {
+            const uint32_t b = __ballot_sync(kFullMask, lev[k] >= l);
+            if (b == 0) break;
+            if ((int)lane == l) my_cnt += __popc(b);
+        }
+    if ((int)lane <= lbits) s_wcnt[warp][lane] = my_cnt;
+    __syncthreads();
+    if ((int)tid <= lbits) {
+        uint32_t run = 0;
+        for (int w = 0; w < kTopoWarps; ++w) {
+            const uint32_t c = s_wcnt[w][tid];
+            s_wcnt[w][tid] = run;
+            run += c;
+        }
+        uint32_t* word = a.lookback + (size_t)tile * 32 + tid;
+        st_relaxed_u32(word, (tile == 0 ? kLbInclusive : kLbAggregate) | run);
+        uint32_t prefix = 0;
+        if (tile > 0) {
+            for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
+                const uint32_t v = lookback_wait(a.lookback + (size_t)j * 32 + tid, a.err);
+                prefix += v & kLbCountMask;
+                if ((v & kLbInclusive) != 0) break;
+            }
+            st_relaxed_u32(word, kLbInclusive | (prefix + run));
+        }
+        s_prefix[tid] = prefix;
+        if (tile == a.ntiles - 1) a.layer_count[tid] = prefix + run;
+    }
+    __syncthreads();
+    uint32_t running = (int)lane <= lbits ? s_prefix[lane] + s_wcnt[warp][lane] : 0u;
+#pragma unroll
+    for (int k = 0; k < kTopoItems; ++k) {
+        const uint32_t i = (uint32_t)(warp_base + 32ull * k + lane);
+        uint32_t idx_below = 0;
+        for (int l = 0; l <= lbits; ++l) {
+            const uint32_t b = __ballot_sync(kFullMask, lev[k] >= l);
+            if (b == 0) break;
+            const uint32_t base_l = __shfl_sync(kFullMask, running, l);
+            if (lev[k] >= l) {
+                const uint32_t idx = base_l + __popc(b & lt);
+                const uint32_t node = s_off[l] + idx;
+                a.pbeg[node] = i;
+                if (l > 0) a.cbeg[node] = s_off[l - 1] + idx_below;
+                idx_below = idx;
+            }
+            if ((int)lane == l) running += __popc(b);
+        }
+    }
+}
+
+// -------------------------------------------------------- aggregation ----
+
+// aggregateLeafNodes (Octree.metal:53-117), one thread per leaf.
+// kMode 0 (REFERENCE): state in upload order, gathered through perm; FP32
+//   sums of m and x*m in sorted order; the last leaf sums [start, numUnique)
+//   as the reference does (Octree.metal:71).
+// kMode 1 (PHYSICAL plain): state already in sorted order; raw FP32 sums.
+// kMode 2 (PHYSICAL precision): FP64 sums of m and m*(x64 - origin).
+template <int kMode>
+__global__ void aggregate_leaf_kernel(AggArgs a) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u0 = a.layer_count[0];
+    if (j >= u0) return;
+    const uint32_t pb = a.pbeg[j];
+    const uint32_t pe = (j + 1 < u0) ? a.pbeg[j + 1] : a.n;
+    const uint64_t key = a.sorted_keys[pb];
+    a.node_key[j] = key;
+    float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (kMode == 0) {
+        const uint32_t sum_end = (j + 1 < u0) ? pe : u0;
+        float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        for (uint32_t i = pb; i < sum_end; ++i) {
+            const float4 q = a.pos[a.perm[i]];
+            m = __fadd_rn(m, q.w);
+            sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
+            sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
+            sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
+        }
+        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
+        else cm.w = m;
+    } else if (kMode == 1) {
+        float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        for (uint32_t i = pb; i < pe; ++i) {
+            const float4 q = a.pos[i];
+            m = __fadd_rn(m, q.w);
+            sx = __fadd_rn(sx, __fmul_rn(q.w, q.x));
+            sy = __fadd_rn(sy, __fmul_rn(q.w, q.y));
+            sz = __fadd_rn(sz, __fmul_rn(q.w, q.z));
+        }
+        reinterpret_cast<float4*>(a.node_sum)[j] = make_float4(sx, sy, sz, m);
+        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
+        else cm.w = m;
+    } else {
+        const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
+        const double ox = a.sys[s].origin[0], oy = a.sys[s].origin[1], oz = a.sys[s].origin[2];
+        double m = 0, sx = 0, sy = 0, sz = 0;
+        for (uint32_t i = pb; i < pe; ++i) {
+            const double mi = (double)a.pos[i].w;
+            m = __dadd_rn(m, mi);
+            sx = __dadd_rn(sx, __dmul_rn(mi, __dsub_rn(a.x64[i], ox)));
+            sy = __dadd_rn(sy, __dmul_rn(mi, __dsub_rn(a.x64[(size_t)a.n + i], oy)));
+            sz = __dadd_rn(sz, __dmul_rn(mi, __dsub_rn(a.x64[2 * (size_t)a.n + i], oz)));
+        }
+        reinterpret_cast<double4*>(a.node_sum)[j] = make_double4(sx, sy, sz, m);
+        if (m > 0.0)
+            cm = make_float4(__double2float_rn(__ddiv_rn(sx, m)), __double2float_rn(__ddiv_rn(sy, m)),
+                             __double2float_rn(__ddiv_rn(sz, m)), __double2float_rn(m));
+        else cm.w = __double2float_rn(m);
+    }
+    a.node_cm[j] = cm;
+    a.node_rng[j] = make_uint4(0u, 0u, pb, pe);
+}
+
+// aggregateNodes (Octree.metal:120-202), one thread per node of layer l.
+// Children are the contiguous run of layer l-1 nodes sharing code >> 3.
+// kMode 0 sums child centre of mass times child mass (the reference's
+// formula); kModes 1 and 2 add the children's raw sums.
+template <int kMode>
+__global__ void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off, uint32_t off_below) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u = a.layer_count[l];
+    if (j >= u) return;
+    const uint32_t node = off + j;
+    const uint32_t cb = a.node_cbeg[node];
+    const uint32_t ce = (j + 1 < u) ? a.node_cbeg[node + 1] : off_below + a.layer_count[l - 1];
+    const uint32_t pb = a.pbeg[node];
+    const uint32_t pe = (j + 1 < u) ? a.pbeg[node + 1] : a.n;
+    a.node_key[node] = a.sorted_keys[pb] >> (3u * l);
+    float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (kMode == 0) {
+        float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        for (uint32_t c = cb; c < ce; ++c) {
+            const float4 q = a.node_cm[c];
+            m = __fadd_rn(m, q.w);
+            sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
+            sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
+            sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
+        }
+        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
+        else cm.w = m;
+    } else if (kMode == 1) {
+        const float4* sum = reinterpret_cast<const float4*>(a.node_sum);
+        float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        for (uint32_t c = cb; c < ce; ++c) {
+            const float4 q = sum[c];
+            sx = __fadd_rn(sx, q.x);
+            sy = __fadd_rn(sy, q.y);
+            sz = __fadd_rn(sz, q.z);
+            m = __fadd_rn(m, q.w);
+        }
+        reinterpret_cast<float4*>(a.node_sum)[node] = make_float4(sx, sy, sz, m);
+        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
+        else cm.w = m;
+    } else {
+        const double4* sum = reinterpret_cast<const double4*>(a.node_sum);
+        double m = 0, sx = 0, sy = 0, sz = 0;
+        for (uint32_t c = cb; c < ce; ++c) {
+            const double4 q = sum[c];
+            sx = __dadd_rn(sx, q.x);
+            sy = __dadd_rn(sy, q.y);
+            sz = __dadd_rn(sz, q.z);
+            m = __dadd_rn(m, q.w);
+        }
+        reinterpret_cast<double4*>(a.node_sum)[node] = make_double4(sx, sy, sz, m);
+        if (m > 0.0)
+            cm = make_float4(__double2float_rn(__ddiv_rn(sx, m)), __double2float_rn(__ddiv_rn(sy, m)),
+                             __double2float_rn(__ddiv_rn(sz, m)), __double2float_rn(m));
+        else cm.w = __double2float_rn(m);
+    }
+    a.node_cm[node] = cm;
+    a.node_rng[node] = make_uint4(cb, ce, pb, pe);
+}
+
+// ---------------------------------------------------------- integrate ----
+
+// updateSpheres (BarnesHut.metal:169-196): a = F * scale[type];
+// v = v * damping + a * dt; x += v * dt.
+__global__ void integrate_ref_kernel(float4* __restrict__ pos, float4* __restrict__ vel,
+                                     const float4* __restrict__ acc,
+                                     const uint32_t* __restrict__ types, uint32_t n, float dt,
+                                     float damping, float s0, float s1, float s2) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = acc[i];
+    const uint32_t t = types[i];
+    if (t <= 2u) {
+        const float s = t == 0 ? s0 : (t == 1 ? s1 : s2);
+        a.x = __fmul_rn(a.x, s);
+        a.y = __fmul_rn(a.y, s);
+        a.z = __fmul_rn(a.z, s);
+    }
+    float4 v = vel[i];
+    v.x = __fadd_rn(__fmul_rn(v.x, damping), __fmul_rn(a.x, dt));
+    v.y = __fadd_rn(__fmul_rn(v.y, damping), __fmul_rn(a.y, dt));
+    v.z = __fadd_rn(__fmul_rn(v.z, damping), __fmul_rn(a.z, dt));
+    vel[i] = v;
+    float4 p = pos[i];
+    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+    pos[i] = p;
+}
+
+// ------------------------------------------------- upload / download -----
+
+template <bool kPrec>
+__global__ void upload_convert_kernel(const PositionMass* __restrict__ pm,
+                                      const VelocityRadius* __restrict__ vr,
+                                      const ColorType* __restrict__ ct, float4* __restrict__ pos,
+                                      float4* __restrict__ vel, uint32_t* __restrict__ ids,
+                                      uint32_t* __restrict__ types, double* __restrict__ x64,
+                                      uint32_t n, uint32_t n_tree) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p0 = *reinterpret_cast<const float4*>(&pm[i].position[0]);
+    const float m = pm[i].mass;
+    const float4 v0 = *reinterpret_cast<const float4*>(&vr[i].velocity[0]);
+    pos[i] = make_float4(p0.x, p0.y, p0.z, m);
+    vel[i] = make_float4(v0.x, v0.y, v0.z, vr[i].radius);
+    if (ids) ids[i] = i;
+    if (types) types[i] = ct ? ct[i].type : (i < n_tree ? 1u : 2u);
+    if (kPrec) {
+        x64[i] = (double)p0.x;
+        x64[(size_t)n + i] = (double)p0.y;
+        x64[2 * (size_t)n + i] = (double)p0.z;
+    }
+}
+
+template <bool kPrec>
+__global__ void download_convert_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                        const uint32_t* __restrict__ ids,
+                                        const double* __restrict__ x64, PositionMass* __restrict__ pm,
+                                        VelocityRadius* __restrict__ vr, uint32_t n) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t i = ids ? ids[j] : j;
+    const float4 p = pos[j], v = vel[j];
+    float4 out_p = make_float4(p.x, p.y, p.z, 0.f);
+    if (kPrec)
+        out_p = make_float4(__double2float_rn(x64[j]), __double2float_rn(x64[(size_t)n + j]),
+                            __double2float_rn(x64[2 * (size_t)n + j]), 0.f);
+    *reinterpret_cast<float4*>(&pm[i].position[0]) = out_p;
+    *reinterpret_cast<float4*>(&pm[i].mass) = make_float4(p.w, 0.f, 0.f, 0.f);
+    *reinterpret_cast<float4*>(&vr[i].velocity[0]) = make_float4(v.x, v.y, v.z, 0.f);
+    *reinterpret_cast<float4*>(&vr[i].radius) = make_float4(v.w, 0.f, 0.f, 0.f);
+}
+
+// Scatter a per-state-slot array back to upload order through ids.
+template <typename T>
+__global__ void scatter_by_id_kernel(const T* __restrict__ src, const uint32_t* __restrict__ ids,
+                                     T* __restrict__ dst, uint32_t n) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    dst[ids ? ids[j] : j] = src[j];
+}
+
+// AoS OctreeNode (bridge.h:47-65) for the slots [first, first+count) of
+// layer l; slots past the live count read as the cleared node
+// (clearOctreeNodeBuffer, Octree.metal:253-269).
+__global__ void readback_nodes_kernel(const float4* __restrict__ node_cm,
+                                      const uint4* __restrict__ node_rng,
+                                      const uint64_t* __restrict__ node_key,
+                                      const uint32_t* __restrict__ layer_count, uint32_t l,
+                                      uint32_t layer_offset, uint32_t first_in_layer,
+                                      uint32_t count, OctreeNode* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t j = first_in_layer + k;
+    OctreeNode o;
+    uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+    for (int q = 0; q < 32; ++q) w[q] = 0;
+    o.mortonCode = ASTRO_INVALID_MORTON_CODE;
+    for (int c = 0; c < 8; ++c) o.children[c] = ASTRO_INVALID_CHILD;
+    if (j < layer_count[l]) {
+        const uint32_t node = layer_offset + j;
+        const float4 cm = node_cm[node];
+        o.mortonCode = node_key[node];
+        o.centerOfMass[0] = cm.x;
+        o.centerOfMass[1] = cm.y;
+        o.centerOfMass[2] = cm.z;
+        o.totalMass = cm.w;
+        o.layer = l;
+        if (l > 0) {
+            const uint4 r = node_rng[node];
+            for (uint32_t c = 0; c < 8 && r.x + c < r.y; ++c) o.children[c] = r.x + c;
+        }
+    }
+    out[k] = o;
+}
+
+// ------------------------------------------------ FP64 direct sum --------
+
+constexpr int kDirectSamples = 8;
+
+// Softened FP64 direct sum for sampled particles (error reference). Each
+// block takes kDirectSamples samples; threads stride over the particles.
+__global__ __launch_bounds__(256) void direct_sum_f64_kernel(DirectArgs a) {
+    __shared__ double s_red[8][kDirectSamples][3];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t first = blockIdx.x * kDirectSamples;
+    double xi[kDirectSamples][3], acc[kDirectSamples][3];
+    uint32_t self[kDirectSamples], lo[kDirectSamples], hi[kDirectSamples];
+    uint32_t glo = 0xFFFFFFFFu, ghi = 0;
+    for (int s = 0; s < kDirectSamples; ++s) {
+        const uint32_t k = first + s;
+        const bool ok = k < a.n_sample;
+        const uint32_t slot = ok ? a.slot[k] : 0u;
+        self[s] = ok ? slot : 0xFFFFFFFFu;
+        lo[s] = ok ? a.sys_begin[k] : 1u;
+        hi[s] = ok ? a.sys_end[k] : 0u;
+        if (ok) {
+            glo = min(glo, lo[s]);
+            ghi = max(ghi, hi[s]);
+        }
+        for (int c = 0; c < 3; ++c) {
+            xi[s][c] = ok ? (a.x64 ? a.x64[(size_t)c * a.n + slot]
+                                   : (double)(&a.pos[slot].x)[c])
+                          : 0.0;
+            acc[s][c] = 0.0;
+        }
+    }
+    for (uint32_t j = glo + tid; j < ghi; j += blockDim.x) {
+        const float4 q = a.pos[j];
+        double xj[3];
+        for (int c = 0; c < 3; ++c)
+            xj[c] = a.x64 ? a.x64[(size_t)c * a.n + j] : (double)(&q.x)[c];
+        const double gm = a.g * (double)q.w;
+        for (int s = 0; s < kDirectSamples; ++s) {
+            if (j < lo[s] || j >= hi[s] || j == self[s]) continue;
+            const double dx = xj[0] - xi[s][0], dy = xj[1] - xi[s][1], dz = xj[2] - xi[s][2];
+            const double r2 = dx * dx + dy * dy + dz * dz + a.eps2;
+            const double inv = 1.0 / sqrt(r2);
+            const double w = gm * inv * inv * inv;
+            acc[s][0] += w * dx;
+            acc[s][1] += w * dy;
+            acc[s][2] += w * dz;
+        }
+    }
+    for (int s = 0; s < kDirectSamples; ++s)
+        for (int c = 0; c < 3; ++c) {
+            double v = acc[s][c];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+            if (lane == 0) s_red[warp][s][c] = v;
+        }
+    __syncthreads();
+    if (tid < kDirectSamples * 3) {
+        const int s = tid / 3, c = tid % 3;
+        double v = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) v += s_red[w][s][c];
+        if (first + s < a.n_sample) a.out[3ull * (first + s) + c] = v;
+    }
+}
+
+__global__ void gather_u32_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
+                                  uint32_t* __restrict__ dst, uint32_t n) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[idx[k]];
+}
+
+__global__ void types_from_colors_kernel(const ColorType* __restrict__ ct, uint32_t* __restrict__ types,
+                                         uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) types[i] = ct[i].type;
+}
+
+// Stand-alone PHYSICAL kick-drift (the same arithmetic as the traversal
+// epilogue): v += a dt, x += v dt, x in FP64 in the precision form.
+template <bool kPrec>
+__global__ void kick_drift_kernel(float4* __restrict__ pos, float4* __restrict__ vel,
+                                  double* __restrict__ x64, const float4* __restrict__ acc,
+                                  uint32_t n, float dt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = acc[i];
+    float4 v = vel[i];
+    v.x = __fadd_rn(v.x, __fmul_rn(a.x, dt));
+    v.y = __fadd_rn(v.y, __fmul_rn(a.y, dt));
+    v.z = __fadd_rn(v.z, __fmul_rn(a.z, dt));
+    vel[i] = v;
+    if (kPrec) {
+        const double ddt = (double)dt;
+        x64[i] = __dadd_rn(x64[i], __dmul_rn((double)v.x, ddt));
+        x64[(size_t)n + i] = __dadd_rn(x64[(size_t)n + i], __dmul_rn((double)v.y, ddt));
+        x64[2 * (size_t)n + i] = __dadd_rn(x64[2 * (size_t)n + i], __dmul_rn((double)v.z, ddt));
+    } else {
+        float4 p = pos[i];
+        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+        pos[i] = p;
+    }
+}
+
+__global__ void inverse_ids_kernel(const uint32_t* __restrict__ ids, uint32_t* __restrict__ inv,
+                                   uint32_t n) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) inv[ids[j]] = j;
+}
+
+// ------------------------------------------------------------ launchers --
+
+namespace {
+inline uint32_t blocks_for(uint64_t n, uint32_t t) { return (uint32_t)((n + t - 1) / t); }
+}  // namespace
+
+cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,
+                              float offset, cudaStream_t st) {
+    if (n_tree == 0) return cudaSuccess;
+    encode_ref_kernel<<<blocks_for(n_tree, 256), 256, 0, st>>>(pos, codes, n_tree, 63u - 3u * lbits,
+                                                               offset);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_encode_phys(bool prec, const Chunk* chunks, uint32_t nchunks, const SysInfo* sys,
+                               float4* pos, const double* x64, uint64_t* codes, uint32_t n,
+                               uint32_t lbits, cudaStream_t st) {
+    if (prec)
+        encode_phys_kernel<true><<<nchunks, 256, 0, st>>>(chunks, sys, pos, x64, codes, n, lbits);
+    else
+        encode_phys_kernel<false><<<nchunks, 256, 0, st>>>(chunks, sys, pos, x64, codes, n, lbits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bbox(bool prec, const Chunk* chunks, uint32_t nchunks, const float4* pos,
+                        const double* x64, uint32_t n, uint32_t* bb32, unsigned long long* bb64,
+                        cudaStream_t st) {
+    if (prec) bbox_kernel<true><<<nchunks, 256, 0, st>>>(chunks, pos, x64, n, bb32, bb64);
+    else bbox_kernel<false><<<nchunks, 256, 0, st>>>(chunks, pos, x64, n, bb32, bb64);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_setup(bool prec, SysInfo* sys, uint32_t nsys, uint32_t* bb32,
+                         unsigned long long* bb64, uint32_t lbits, float theta, uint32_t root_offset,
+                         cudaStream_t st) {
+    if (prec)
+        setup_kernel<true><<<blocks_for(nsys, 128), 128, 0, st>>>(sys, nsys, bb32, bb64, lbits,
+                                                                  theta, root_offset);
+    else
+        setup_kernel<false><<<blocks_for(nsys, 128), 128, 0, st>>>(sys, nsys, bb32, bb64, lbits,
+                                                                   theta, root_offset);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reorder(bool prec, const uint32_t* perm, const float4* pos_a, const float4* vel_a,
+                           const uint32_t* id_a, const double* x_a, float4* pos_b, float4* vel_b,
+                           uint32_t* id_b, double* x_b, uint32_t n, cudaStream_t st) {
+    if (prec)
+        reorder_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(perm, pos_a, vel_a, id_a, x_a,
+                                                                 pos_b, vel_b, id_b, x_b, n);
+    else
+        reorder_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(perm, pos_a, vel_a, id_a, x_a,
+                                                                  pos_b, vel_b, id_b, x_b, n);
+    return cudaGetLastError();
+}
+
+uint32_t topology_tiles(uint32_t n) { return blocks_for(n, kTopoTile); }
+
+cudaError_t launch_topology(const TopoArgs& a, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    topology_kernel<<<a.ntiles, kTopoThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aggregate(int mode, const AggArgs& a, const LayerTable& t, cudaStream_t st) {
+    const uint32_t t0 = 128;
+    if (mode == 0) aggregate_leaf_kernel<0><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
+    else if (mode == 1) aggregate_leaf_kernel<1><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
+    else aggregate_leaf_kernel<2><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
+    for (uint32_t l = 1; l < t.n_layers; ++l) {
+        const uint32_t g = blocks_for(t.size[l], t0);
+        if (mode == 0)
+            aggregate_internal_kernel<0><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
+        else if (mode == 1)
+            aggregate_internal_kernel<1><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
+        else
+            aggregate_internal_kernel<2><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_integrate_ref(float4* pos, float4* vel, const float4* acc, const uint32_t* types,
+                                 uint32_t n, float dt, const astro_params& p, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    integrate_ref_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
+        pos, vel, acc, types, n, dt, p.damping, p.type_accel_scale[0], p.type_accel_scale[1],
+        p.type_accel_scale[2]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_upload_convert(bool prec, const PositionMass* pm, const VelocityRadius* vr,
+                                  const ColorType* ct, float4* pos, float4* vel, uint32_t* ids,
+                                  uint32_t* types, double* x64, uint32_t n, uint32_t n_tree,
+                                  cudaStream_t st) {
+    if (prec)
+        upload_convert_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(pm, vr, ct, pos, vel, ids,
+                                                                        types, x64, n, n_tree);
+    else
+        upload_convert_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(pm, vr, ct, pos, vel, ids,
+                                                                         types, x64, n, n_tree);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_download_convert(bool prec, const float4* pos, const float4* vel,
+                                    const uint32_t* ids, const double* x64, PositionMass* pm,
+                                    VelocityRadius* vr, uint32_t n, cudaStream_t st) {
+    if (prec)
+        download_convert_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, ids, x64, pm,
+                                                                          vr, n);
+    else
+        download_convert_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, ids, x64, pm,
+                                                                           vr, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_u64(const uint64_t* src, const uint32_t* ids, uint64_t* dst, uint32_t n,
+                               cudaStream_t st) {
+    scatter_by_id_kernel<uint64_t><<<blocks_for(n, 256), 256, 0, st>>>(src, ids, dst, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_scatter_f4(const float4* src, const uint32_t* ids, float4* dst, uint32_t n,
+                              cudaStream_t st) {
+    scatter_by_id_kernel<float4><<<blocks_for(n, 256), 256, 0, st>>>(src, ids, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_readback_nodes(const float4* cm, const uint4* rng, const uint64_t* key,
+                                  const uint32_t* layer_count, uint32_t l, uint32_t layer_offset,
+                                  uint32_t first_in_layer, uint32_t count, OctreeNode* out,
+                                  cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    readback_nodes_kernel<<<blocks_for(count, 128), 128, 0, st>>>(
+        cm, rng, key, layer_count, l, layer_offset, first_in_layer, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_direct_sum(const DirectArgs& a, cudaStream_t st) {
+    if (a.n_sample == 0) return cudaSuccess;
+    direct_sum_f64_kernel<<<blocks_for(a.n_sample, kDirectSamples), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inverse_ids(const uint32_t* ids, uint32_t* inv, uint32_t n, cudaStream_t st) {
+    inverse_ids_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ids, inv, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t* dst, uint32_t n,
+                              cudaStream_t st) {
+    gather_u32_kernel<<<blocks_for(n, 256), 256, 0, st>>>(src, idx, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, uint32_t n,
+                                     cudaStream_t st) {
+    types_from_colors_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ct, types, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kick_drift(bool prec, float4* pos, float4* vel, double* x64, const float4* acc,
+                              uint32_t n, float dt, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    if (prec) kick_drift_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, x64, acc, n, dt);
+    else kick_drift_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, x64, acc, n, dt);
+    return cudaGetLastError();
+}
+
+}  // namespace astro

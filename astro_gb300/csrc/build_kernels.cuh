@@ -1,0 +1,144 @@
+// Argument blocks and launchers of the pipeline kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace astro {
+
+struct TopoArgs {
+    const uint64_t* keys;
+    uint32_t n;
+    uint32_t lbits;
+    uint32_t ntiles;
+    uint32_t offset[ASTRO_MAX_LAYERS];
+    uint32_t* pbeg;
+    uint32_t* cbeg;
+    uint32_t* layer_count;
+    uint32_t* lookback;  // [ntiles][32] status words
+    uint32_t* tile_counter;
+    uint32_t* err;
+};
+
+struct AggArgs {
+    const uint64_t* sorted_keys;
+    const uint32_t* perm;      // REFERENCE: sorted slot -> upload index
+    const float4* pos;         // REFERENCE: upload order; PHYSICAL: sorted order
+    const double* x64;         // precision form, sorted order
+    const SysInfo* sys;
+    const uint32_t* pbeg;
+    const uint32_t* node_cbeg;
+    const uint32_t* layer_count;
+    float4* node_cm;
+    uint4* node_rng;
+    uint64_t* node_key;
+    void* node_sum;
+    uint32_t n;
+    uint32_t lbits;
+};
+
+struct DirectArgs {
+    const float4* pos;
+    const double* x64;
+    const uint32_t* slot;       // state slot of each sample
+    const uint32_t* sys_begin;  // its system's slot range
+    const uint32_t* sys_end;
+    double* out;
+    uint32_t n;
+    uint32_t n_sample;
+    double g;
+    double eps2;
+};
+
+struct TraverseArgs {
+    const float4* node_cm;
+    const uint4* node_rng;
+    const uint64_t* node_key;
+    const SysInfo* sys;
+    const float4* pos;          // positions the forces are evaluated at
+    const uint64_t* sorted_keys;
+    float4* acc;
+    // PHYSICAL epilogue: kick-drift from the B buffers into the A buffers.
+    const float4* vel_in;
+    float4* vel_out;
+    float4* pos_out;
+    const uint32_t* id_in;
+    uint32_t* id_out;
+    const double* x64_in;
+    double* x64_out;
+    // REFERENCE: own key for the self-leaf test, particle types.
+    const uint64_t* codes;
+    const uint32_t* types;
+    uint32_t n_tree;
+    uint32_t n;
+    uint32_t lbits;
+    uint32_t root;
+    uint32_t bucket;
+    float g;
+    float eps2;          // PHYSICAL eps^2; REFERENCE softening added to r^2
+    float clampv;
+    float dt;
+    float theta;
+    float leaf_min_dist2;
+    uint32_t* err;
+    unsigned long long* stats;
+    uint32_t* queue;
+};
+
+cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,
+                              float offset, cudaStream_t st);
+cudaError_t launch_encode_phys(bool prec, const Chunk* chunks, uint32_t nchunks, const SysInfo* sys,
+                               float4* pos, const double* x64, uint64_t* codes, uint32_t n,
+                               uint32_t lbits, cudaStream_t st);
+cudaError_t launch_bbox(bool prec, const Chunk* chunks, uint32_t nchunks, const float4* pos,
+                        const double* x64, uint32_t n, uint32_t* bb32, unsigned long long* bb64,
+                        cudaStream_t st);
+cudaError_t launch_setup(bool prec, SysInfo* sys, uint32_t nsys, uint32_t* bb32,
+                         unsigned long long* bb64, uint32_t lbits, float theta, uint32_t root_offset,
+                         cudaStream_t st);
+cudaError_t launch_reorder(bool prec, const uint32_t* perm, const float4* pos_a, const float4* vel_a,
+                           const uint32_t* id_a, const double* x_a, float4* pos_b, float4* vel_b,
+                           uint32_t* id_b, double* x_b, uint32_t n, cudaStream_t st);
+uint32_t topology_tiles(uint32_t n);
+cudaError_t launch_topology(const TopoArgs& a, cudaStream_t st);
+cudaError_t launch_aggregate(int mode, const AggArgs& a, const LayerTable& t, cudaStream_t st);
+cudaError_t launch_integrate_ref(float4* pos, float4* vel, const float4* acc, const uint32_t* types,
+                                 uint32_t n, float dt, const astro_params& p, cudaStream_t st);
+cudaError_t launch_upload_convert(bool prec, const PositionMass* pm, const VelocityRadius* vr,
+                                  const ColorType* ct, float4* pos, float4* vel, uint32_t* ids,
+                                  uint32_t* types, double* x64, uint32_t n, uint32_t n_tree,
+                                  cudaStream_t st);
+cudaError_t launch_download_convert(bool prec, const float4* pos, const float4* vel,
+                                    const uint32_t* ids, const double* x64, PositionMass* pm,
+                                    VelocityRadius* vr, uint32_t n, cudaStream_t st);
+cudaError_t launch_scatter_u64(const uint64_t* src, const uint32_t* ids, uint64_t* dst, uint32_t n,
+                               cudaStream_t st);
+cudaError_t launch_scatter_f4(const float4* src, const uint32_t* ids, float4* dst, uint32_t n,
+                              cudaStream_t st);
+cudaError_t launch_readback_nodes(const float4* cm, const uint4* rng, const uint64_t* key,
+                                  const uint32_t* layer_count, uint32_t l, uint32_t layer_offset,
+                                  uint32_t first_in_layer, uint32_t count, OctreeNode* out,
+                                  cudaStream_t st);
+cudaError_t launch_direct_sum(const DirectArgs& a, cudaStream_t st);
+cudaError_t launch_inverse_ids(const uint32_t* ids, uint32_t* inv, uint32_t n, cudaStream_t st);
+cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t* dst, uint32_t n,
+                              cudaStream_t st);
+cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, uint32_t n,
+                                     cudaStream_t st);
+cudaError_t launch_kick_drift(bool prec, float4* pos, float4* vel, double* x64, const float4* acc,
+                              uint32_t n, float dt, cudaStream_t st);
+
+// Traversal (traverse.cu).
+struct TraverseConfig {
+    bool exact;       // correctly rounded arithmetic (reproduces the CPU restatement)
+    bool precision;   // compensated sums, FP64 drift
+    bool batched;     // several systems: per-lane system and root
+    bool persistent;  // persistent blocks with a work-stealing chunk queue
+    int warps;        // warps per block (2, 4 or 8)
+};
+cudaError_t launch_traverse_ref(const TraverseArgs& a, cudaStream_t st);
+cudaError_t launch_traverse_phys(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
+
+}  // namespace astro

@@ -1,0 +1,875 @@
+// libastro_cuda context and C ABI (include/astro_cuda.h).
+//
+// The context plays the role of the reference Renderer's compute state
+// (Astro/Renderer.swift:56-70,336-391) and its per-frame compute section
+// (Renderer.draw, Renderer.swift:495-542), on one CUDA stream:
+//
+// REFERENCE step: encode (codes by particle) -> sort -> topology ->
+//   aggregate (perm gathers) -> traverse (per particle) -> integrate.
+// PHYSICAL step: bbox -> setup -> encode -> sort -> reorder the state into
+//   Morton order -> topology -> aggregate -> traverse with the kick-drift
+//   fused into its epilogue. The state stays in Morton order between steps
+//   (buffer A); ids map it back to upload order for downloads and readbacks.
+//   astro_step replays the step as a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "build_kernels.cuh"
+#include "common.cuh"
+#include "internal.h"
+
+using astro::Chunk;
+using astro::LayerTable;
+using astro::SysInfo;
+
+namespace {
+
+constexpr const char* kVersion = "astro_gb300 1.0 (sm_103a)";
+
+int fail(astro_ctx* ctx, int code, const char* what) {
+    if (ctx) ctx->last_error = what;
+    return code;
+}
+
+int cuda_fail(astro_ctx* ctx, cudaError_t e, const char* where) {
+    if (ctx) {
+        ctx->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    }
+    (void)cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? ASTRO_ERR_OUT_OF_MEMORY : ASTRO_ERR_CUDA;
+}
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+template <typename T>
+cudaError_t dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+template <typename T>
+void dev_free(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+bool is_phys(const astro_ctx* ctx) { return ctx->p.preset == ASTRO_PRESET_PHYSICAL; }
+bool is_prec(const astro_ctx* ctx) { return is_phys(ctx) && ctx->p.form == ASTRO_FORM_PRECISION; }
+
+uint32_t bits_for(uint32_t nsys) {
+    uint32_t b = 0;
+    while ((1ull << b) < nsys) ++b;
+    return b;
+}
+
+int validate_params(const astro_params* p, const char** why) {
+    if (!p) return (*why = "params is NULL", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->preset > ASTRO_PRESET_PHYSICAL) return (*why = "unknown preset", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->form > ASTRO_FORM_PRECISION) return (*why = "unknown form", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->form == ASTRO_FORM_PRECISION && p->preset != ASTRO_PRESET_PHYSICAL)
+        return (*why = "the precision form needs the PHYSICAL preset", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->lbits < 1 || p->lbits > ASTRO_MAX_LBITS)
+        return (*why = "lbits must be in [1, 21]", ASTRO_ERR_INVALID_ARGUMENT);
+    if (!(p->theta > 0.0f) || !std::isfinite(p->theta))
+        return (*why = "theta must be positive", ASTRO_ERR_INVALID_ARGUMENT);
+    if (!std::isfinite(p->g) || !std::isfinite(p->softening) || p->softening < 0.0f)
+        return (*why = "g and softening must be finite, softening >= 0", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->block_warps != 0 && p->block_warps != 2 && p->block_warps != 4 && p->block_warps != 8)
+        return (*why = "block_warps must be 0, 2, 4 or 8", ASTRO_ERR_INVALID_ARGUMENT);
+    return ASTRO_OK;
+}
+
+// Closed-form layer capacity (Renderer.swift:373-386) summed over systems.
+void layer_table(const std::vector<uint32_t>& sizes, uint32_t lbits, LayerTable* t,
+                 uint64_t* capacity) {
+    std::memset(t, 0, sizeof(*t));
+    t->n_layers = lbits + 1;
+    uint64_t off = 0;
+    for (uint32_t l = 0; l <= lbits; ++l) {
+        const uint32_t bits = 3u * (lbits - l);
+        const uint64_t possible = bits >= 40 ? (1ull << 40) : (1ull << bits);
+        uint64_t size = 0;
+        for (uint32_t s : sizes) size += std::min<uint64_t>(s, possible);
+        t->size[l] = (uint32_t)size;
+        t->offset[l] = (uint32_t)off;
+        off += size;
+    }
+    *capacity = off;
+}
+
+int ensure_tree(astro_ctx* ctx, uint64_t capacity) {
+    if (capacity <= ctx->tree_capacity) return ASTRO_OK;
+    if (capacity >= (1ull << 32)) return fail(ctx, ASTRO_ERR_CAPACITY, "node capacity exceeds 2^32");
+    dev_free(ctx->node_cm);
+    dev_free(ctx->node_rng);
+    dev_free(ctx->node_key);
+    if (ctx->node_sum) cudaFree(ctx->node_sum);
+    ctx->node_sum = nullptr;
+    dev_free(ctx->node_pbeg);
+    dev_free(ctx->node_cbeg);
+    ctx->tree_capacity = 0;
+    const uint64_t cap = capacity;
+    CK(dev_alloc(&ctx->node_cm, cap));
+    CK(dev_alloc(&ctx->node_rng, cap));
+    CK(dev_alloc(&ctx->node_key, cap));
+    CK(cudaMalloc(&ctx->node_sum, cap * 32));  // room for double4 sums
+    CK(dev_alloc(&ctx->node_pbeg, cap + 1));
+    CK(dev_alloc(&ctx->node_cbeg, cap + 1));
+    ctx->tree_capacity = cap;
+    return ASTRO_OK;
+}
+
+int ensure_x64(astro_ctx* ctx) {
+    if (ctx->x64[0]) return ASTRO_OK;
+    CK(dev_alloc(&ctx->x64[0], 3ull * ctx->max_n));
+    CK(dev_alloc(&ctx->x64[1], 3ull * ctx->max_n));
+    return ASTRO_OK;
+}
+
+// Read and clear the device error word (waits for the stream).
+int check_device(astro_ctx* ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, ctx->err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) {
+        CK(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
+        if (err & astro::kErrLookbackTimeout)
+            return fail(ctx, ASTRO_ERR_DEVICE_TIMEOUT, "a decoupled look-back wait gave up");
+        return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW, "a traversal stack bound was hit");
+    }
+    return ASTRO_OK;
+}
+
+// Buffers holding the current PHYSICAL state: A between steps, B after
+// astro_sort until the traversal writes A back.
+struct Cur {
+    float4* pos;
+    float4* vel;
+    uint32_t* ids;
+    double* x64;
+};
+Cur current(astro_ctx* ctx) {
+    const int b = ctx->state_in_b ? 1 : 0;
+    return Cur{ctx->pos[b], ctx->vel[b], is_phys(ctx) ? ctx->ids[b] : nullptr, ctx->x64[b]};
+}
+
+astro::TraverseConfig traverse_config(const astro_ctx* ctx) {
+    astro::TraverseConfig c;
+    c.exact = (ctx->p.flags & ASTRO_FLAG_IEEE_EXACT) != 0;
+    c.precision = is_prec(ctx);
+    c.batched = ctx->nsys > 1;
+    c.persistent = (ctx->p.flags & ASTRO_FLAG_PERSISTENT) != 0;
+    c.warps = ctx->p.block_warps ? (int)ctx->p.block_warps : 4;
+    return c;
+}
+
+// --------------------------------------------------------------- stages --
+
+int stage_encode(astro_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    if (!is_phys(ctx)) {
+        CK(astro::launch_encode_ref(ctx->pos[0], ctx->codes, ctx->n_tree, ctx->lbits,
+                                    ctx->p.quant_offset, st));
+        return ASTRO_OK;
+    }
+    if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "encode called between sort and traverse");
+    const bool prec = is_prec(ctx);
+    CK(astro::launch_bbox(prec, ctx->chunks, ctx->nchunks, ctx->pos[0], ctx->x64[0], ctx->n,
+                          ctx->bbox32, ctx->bbox64, st));
+    CK(astro::launch_setup(prec, ctx->sys, ctx->nsys, ctx->bbox32, ctx->bbox64, ctx->lbits,
+                           ctx->p.theta, ctx->layers.offset[ctx->lbits], st));
+    CK(astro::launch_encode_phys(prec, ctx->chunks, ctx->nchunks, ctx->sys, ctx->pos[0],
+                                 ctx->x64[0], ctx->codes, ctx->n, ctx->lbits, st));
+    return ASTRO_OK;
+}
+
+int stage_sort(astro_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t count = is_phys(ctx) ? ctx->n : ctx->n_tree;
+    CK(astro::sort_pairs(ctx->codes, nullptr, ctx->sorted_keys, ctx->perm, count, nullptr,
+                         ctx->key_bits, ctx->sort_temp, ctx->sort_temp_bytes, st, ctx->err));
+    if (is_phys(ctx)) {
+        if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "sort called twice without traverse");
+        CK(astro::launch_reorder(is_prec(ctx), ctx->perm, ctx->pos[0], ctx->vel[0], ctx->ids[0],
+                                 ctx->x64[0], ctx->pos[1], ctx->vel[1], ctx->ids[1], ctx->x64[1],
+                                 ctx->n, st));
+        ctx->state_in_b = true;
+    }
+    return ASTRO_OK;
+}
+
+int stage_build(astro_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t count = is_phys(ctx) ? ctx->n : ctx->n_tree;
+    if (count == 0) return ASTRO_OK;
+    if (is_phys(ctx) && !ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "build called before sort");
+    astro::TopoArgs t{};
+    t.keys = ctx->sorted_keys;
+    t.n = count;
+    t.lbits = ctx->lbits;
+    t.ntiles = astro::topology_tiles(count);
+    for (uint32_t l = 0; l <= ctx->lbits; ++l) t.offset[l] = ctx->layers.offset[l];
+    t.pbeg = ctx->node_pbeg;
+    t.cbeg = ctx->node_cbeg;
+    t.layer_count = ctx->layer_count;
+    t.lookback = ctx->topo_lookback;
+    t.tile_counter = ctx->counters;
+    t.err = ctx->err;
+    CK(cudaMemsetAsync(ctx->topo_lookback, 0, (size_t)t.ntiles * 32 * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(ctx->counters, 0, sizeof(uint32_t), st));
+    CK(astro::launch_topology(t, st));
+    astro::AggArgs a{};
+    a.sorted_keys = ctx->sorted_keys;
+    a.perm = ctx->perm;
+    a.pos = is_phys(ctx) ? ctx->pos[1] : ctx->pos[0];
+    a.x64 = ctx->x64[1];
+    a.sys = ctx->sys;
+    a.pbeg = ctx->node_pbeg;
+    a.node_cbeg = ctx->node_cbeg;
+    a.layer_count = ctx->layer_count;
+    a.node_cm = ctx->node_cm;
+    a.node_rng = ctx->node_rng;
+    a.node_key = ctx->node_key;
+    a.node_sum = ctx->node_sum;
+    a.n = count;
+    a.lbits = ctx->lbits;
+    const int mode = !is_phys(ctx) ? 0 : (is_prec(ctx) ? 2 : 1);
+    CK(astro::launch_aggregate(mode, a, ctx->layers, st));
+    ctx->tree_valid = true;
+    return ASTRO_OK;
+}
+
+astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
+    astro::TraverseArgs a{};
+    a.node_cm = ctx->node_cm;
+    a.node_rng = ctx->node_rng;
+    a.node_key = ctx->node_key;
+    a.sys = ctx->sys;
+    a.sorted_keys = ctx->sorted_keys;
+    a.acc = ctx->acc;
+    a.n_tree = ctx->n_tree;
+    a.n = ctx->n;
+    a.lbits = ctx->lbits;
+    a.root = ctx->layers.offset[ctx->lbits];
+    a.bucket = ctx->p.bucket;
+    a.g = ctx->p.g;
+    a.clampv = ctx->p.force_clamp;
+    a.dt = integrate ? dt : 0.0f;
+    a.theta = ctx->p.theta;
+    a.leaf_min_dist2 = ctx->p.leaf_min_dist2;
+    a.err = ctx->err;
+    a.stats = ctx->stats;
+    a.queue = ctx->counters + 1;
+    if (is_phys(ctx)) {
+        a.eps2 = ctx->p.softening * ctx->p.softening;
+        a.pos = ctx->pos[1];
+        a.vel_in = ctx->vel[1];
+        a.vel_out = ctx->vel[0];
+        a.pos_out = ctx->pos[0];
+        a.id_in = ctx->ids[1];
+        a.id_out = ctx->ids[0];
+        a.x64_in = ctx->x64[1];
+        a.x64_out = ctx->x64[0];
+    } else {
+        a.eps2 = ctx->p.softening;
+        a.pos = ctx->pos[0];
+        a.codes = ctx->codes;
+        a.types = ctx->types;
+    }
+    return a;
+}
+
+// PHYSICAL: dt > 0 fuses the kick-drift into the traversal; dt == 0 only
+// evaluates forces (the state is copied back to A unchanged).
+int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(ctx->stats, 0, 2 * sizeof(unsigned long long), st));
+    if (!is_phys(ctx)) {
+        if (ctx->n_tree == 0) {
+            CK(cudaMemsetAsync(ctx->acc, 0, sizeof(float4) * ctx->n, st));
+            return ASTRO_OK;
+        }
+        if (!ctx->tree_valid) return fail(ctx, ASTRO_ERR_STATE, "traverse called before build");
+        CK(astro::launch_traverse_ref(traverse_args(ctx, 0.0f, false), st));
+        return ASTRO_OK;
+    }
+    if (!ctx->state_in_b || !ctx->tree_valid)
+        return fail(ctx, ASTRO_ERR_STATE, "traverse called before sort and build");
+    CK(astro::launch_traverse_phys(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
+    ctx->state_in_b = false;
+    return ASTRO_OK;
+}
+
+int stage_integrate(astro_ctx* ctx, float dt) {
+    if (!is_phys(ctx)) {
+        CK(astro::launch_integrate_ref(ctx->pos[0], ctx->vel[0], ctx->acc, ctx->types, ctx->n, dt,
+                                       ctx->p, ctx->stream));
+        return ASTRO_OK;
+    }
+    if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "integrate called before traverse");
+    CK(astro::launch_kick_drift(is_prec(ctx), ctx->pos[0], ctx->vel[0], ctx->x64[0], ctx->acc,
+                                ctx->n, dt, ctx->stream));
+    return ASTRO_OK;
+}
+
+int run_step(astro_ctx* ctx, float dt) {
+    int r;
+    if ((r = stage_encode(ctx)) != ASTRO_OK) return r;
+    if ((r = stage_sort(ctx)) != ASTRO_OK) return r;
+    if ((r = stage_build(ctx)) != ASTRO_OK) return r;
+    if (is_phys(ctx)) return stage_traverse(ctx, dt, true);
+    if ((r = stage_traverse(ctx, 0.0f, false)) != ASTRO_OK) return r;
+    return stage_integrate(ctx, dt);
+}
+
+void drop_graph(astro_ctx* ctx) {
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    ctx->graph_valid = false;
+}
+
+int capture_step(astro_ctx* ctx, float dt) {
+    drop_graph(ctx);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int r = run_step(ctx, dt);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (r != ASTRO_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    ctx->graph_valid = true;
+    ctx->graph_dt = dt;
+    return ASTRO_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI --
+
+extern "C" {
+
+const char* astro_version(void) { return kVersion; }
+
+const char* astro_status_string(int status) {
+    switch (status) {
+        case ASTRO_OK: return "ok";
+        case ASTRO_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ASTRO_ERR_CAPACITY: return "capacity exceeded";
+        case ASTRO_ERR_CUDA: return "CUDA error";
+        case ASTRO_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case ASTRO_ERR_STATE: return "call order violated";
+        case ASTRO_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+        case ASTRO_ERR_NOT_SUPPORTED: return "not supported";
+        case ASTRO_ERR_DEVICE_OVERFLOW: return "device-side bound exceeded";
+        default: return "unknown status";
+    }
+}
+
+const char* astro_last_error(const astro_ctx* ctx) {
+    return ctx ? ctx->last_error.c_str() : "no context";
+}
+
+int astro_params_default(uint32_t preset, astro_params* out) {
+    if (!out) return ASTRO_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->preset = preset;
+    out->form = ASTRO_FORM_PLAIN;
+    out->lbits = 6;                 // MortonCode.metal:47-50
+    out->theta = 0.7f;              // Renderer.swift:864
+    out->force_clamp = 1e5f;        // BarnesHut.metal:100
+    if (preset == ASTRO_PRESET_REFERENCE) {
+        out->g = 1e11f;             // BarnesHut.metal:39
+        out->softening = 0.01f;     // BarnesHut.metal:40
+        out->leaf_min_dist2 = 50.0f;// BarnesHut.metal:70
+        out->quant_offset = 1e6f;   // MortonCode.metal:35-37
+        out->damping = 0.9995f;     // BarnesHut.metal:189
+        out->type_accel_scale[0] = 5.0f;  // BarnesHut.metal:181-187
+        out->type_accel_scale[1] = 5.0f;
+        out->type_accel_scale[2] = 1.0f;
+        out->bucket = 0;
+    } else if (preset == ASTRO_PRESET_PHYSICAL) {
+        out->g = 1.0f;
+        out->softening = 0.01f;
+        out->damping = 1.0f;
+        out->type_accel_scale[0] = out->type_accel_scale[1] = out->type_accel_scale[2] = 1.0f;
+        out->bucket = 16;
+    } else {
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    }
+    return ASTRO_OK;
+}
+
+int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_systems,
+                 astro_ctx** out) {
+    if (!out) return ASTRO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    const char* why = nullptr;
+    int r = validate_params(params, &why);
+    if (r != ASTRO_OK) return r;
+    if (max_n == 0 || max_n > (1u << 30) || max_systems == 0 || max_systems > ASTRO_MAX_SYSTEMS)
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    astro_ctx* ctx = new (std::nothrow) astro_ctx();
+    if (!ctx) return ASTRO_ERR_OUT_OF_MEMORY;
+    ctx->p = *params;
+    ctx->max_n = max_n;
+    ctx->max_sys = max_systems;
+    auto cleanup = [&](int code) {
+        astro_destroy(ctx);
+        return code;
+    };
+#define CKC(call)                                          \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cleanup(cuda_fail(nullptr, e_, #call)); \
+    } while (0)
+    CKC(cudaGetDevice(&ctx->device));
+    CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        CKC(dev_alloc(&ctx->pos[b], max_n));
+        CKC(dev_alloc(&ctx->vel[b], max_n));
+        CKC(dev_alloc(&ctx->ids[b], max_n));
+    }
+    CKC(dev_alloc(&ctx->acc, max_n));
+    CKC(dev_alloc(&ctx->types, max_n));
+    CKC(dev_alloc(&ctx->codes, max_n));
+    CKC(dev_alloc(&ctx->sorted_keys, max_n));
+    CKC(dev_alloc(&ctx->perm, max_n));
+    ctx->staging_bytes = 64ull * max_n + 4096;
+    CKC(cudaMalloc(&ctx->staging, ctx->staging_bytes));
+    ctx->sort_temp_bytes = astro::sort_plan(max_n, 64).total;
+    CKC(cudaMalloc(&ctx->sort_temp, ctx->sort_temp_bytes));
+    ctx->topo_lookback_words = (size_t)astro::topology_tiles(max_n) * 32 + 32;
+    CKC(dev_alloc(&ctx->topo_lookback, ctx->topo_lookback_words));
+    CKC(dev_alloc(&ctx->counters, 16));
+    CKC(dev_alloc(&ctx->err, 1));
+    CKC(dev_alloc(&ctx->stats, 2));
+    CKC(dev_alloc(&ctx->layer_count, ASTRO_MAX_LAYERS));
+    CKC(dev_alloc(&ctx->sys, max_systems));
+    CKC(dev_alloc(&ctx->bbox32, 6ull * max_systems));
+    CKC(dev_alloc(&ctx->bbox64, 6ull * max_systems));
+    ctx->chunk_capacity = max_n / astro::kChunkParticles + max_systems + 1;
+    CKC(dev_alloc(&ctx->chunks, ctx->chunk_capacity));
+    CKC(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
+    CKC(cudaMemset(ctx->layer_count, 0, sizeof(uint32_t) * ASTRO_MAX_LAYERS));
+    CKC(cudaMemset(ctx->stats, 0, 2 * sizeof(unsigned long long)));
+    if (params->form == ASTRO_FORM_PRECISION && ensure_x64(ctx) != ASTRO_OK)
+        return cleanup(ASTRO_ERR_OUT_OF_MEMORY);
+#undef CKC
+    *out = ctx;
+    return ASTRO_OK;
+}
+
+int astro_destroy(astro_ctx* ctx) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    for (int b = 0; b < 2; ++b) {
+        dev_free(ctx->pos[b]);
+        dev_free(ctx->vel[b]);
+        dev_free(ctx->ids[b]);
+        dev_free(ctx->x64[b]);
+    }
+    dev_free(ctx->acc);
+    dev_free(ctx->types);
+    dev_free(ctx->codes);
+    dev_free(ctx->sorted_keys);
+    dev_free(ctx->perm);
+    if (ctx->staging) cudaFree(ctx->staging);
+    if (ctx->sort_temp) cudaFree(ctx->sort_temp);
+    dev_free(ctx->topo_lookback);
+    dev_free(ctx->counters);
+    dev_free(ctx->err);
+    dev_free(ctx->stats);
+    dev_free(ctx->layer_count);
+    dev_free(ctx->sys);
+    dev_free(ctx->bbox32);
+    dev_free(ctx->bbox64);
+    dev_free(ctx->chunks);
+    dev_free(ctx->node_cm);
+    dev_free(ctx->node_rng);
+    dev_free(ctx->node_key);
+    if (ctx->node_sum) cudaFree(ctx->node_sum);
+    dev_free(ctx->node_pbeg);
+    dev_free(ctx->node_cbeg);
+    if (ctx->readback) cudaFree(ctx->readback);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ASTRO_OK;
+}
+
+int astro_get_params(const astro_ctx* ctx, astro_params* out) {
+    if (!ctx || !out) return ASTRO_ERR_INVALID_ARGUMENT;
+    *out = ctx->p;
+    return ASTRO_OK;
+}
+
+// Changing preset, form or lbits discards the uploaded state (upload again);
+// the other fields take effect at the next step.
+int astro_set_params(astro_ctx* ctx, const astro_params* params) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    const char* why = nullptr;
+    int r = validate_params(params, &why);
+    if (r != ASTRO_OK) return fail(ctx, r, why);
+    const bool structural = params->preset != ctx->p.preset || params->form != ctx->p.form ||
+                            params->lbits != ctx->p.lbits;
+    if (params->form == ASTRO_FORM_PRECISION && (r = ensure_x64(ctx)) != ASTRO_OK) return r;
+    ctx->p = *params;
+    drop_graph(ctx);
+    if (structural) {
+        ctx->uploaded = false;
+        ctx->tree_valid = false;
+        ctx->state_in_b = false;
+    }
+    return ASTRO_OK;
+}
+
+static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                         const ColorType* ct, uint32_t n, uint32_t n_tree,
+                         const std::vector<uint32_t>& sizes) {
+    cudaStream_t st = ctx->stream;
+    const bool phys = is_phys(ctx), prec = is_prec(ctx);
+    drop_graph(ctx);
+    ctx->uploaded = false;
+    ctx->tree_valid = false;
+    ctx->state_in_b = false;
+    ctx->n = n;
+    ctx->n_tree = n_tree;
+    ctx->nsys = (uint32_t)sizes.size();
+    ctx->lbits = ctx->p.lbits;
+    ctx->sysbits = ctx->nsys > 1 ? bits_for(ctx->nsys) : 0;
+    ctx->key_bits = 3 * ctx->lbits + ctx->sysbits;
+    if (ctx->key_bits > 64)
+        return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "3*lbits + system bits exceeds 64 key bits");
+    layer_table(sizes, ctx->lbits, &ctx->layers, &ctx->capacity);
+    int r = ensure_tree(ctx, ctx->capacity);
+    if (r != ASTRO_OK) return r;
+    if (prec && (r = ensure_x64(ctx)) != ASTRO_OK) return r;
+    // Systems and chunks.
+    std::vector<SysInfo> sys(ctx->nsys);
+    std::vector<Chunk> chunks;
+    uint32_t off = 0;
+    for (uint32_t s = 0; s < ctx->nsys; ++s) {
+        std::memset(&sys[s], 0, sizeof(SysInfo));
+        sys[s].begin = off;
+        sys[s].end = off + sizes[s];
+        sys[s].root = ctx->layers.offset[ctx->lbits] + s;
+        for (uint32_t b = off; b < off + sizes[s]; b += astro::kChunkParticles)
+            chunks.push_back(Chunk{s, b, std::min(b + astro::kChunkParticles, off + sizes[s]), 0});
+        off += sizes[s];
+    }
+    if (chunks.size() > ctx->chunk_capacity) return fail(ctx, ASTRO_ERR_CAPACITY, "too many chunks");
+    ctx->nchunks = (uint32_t)chunks.size();
+    ctx->sys_sizes = sizes;
+    CK(cudaMemcpyAsync(ctx->sys, sys.data(), sizeof(SysInfo) * sys.size(), cudaMemcpyHostToDevice, st));
+    if (!chunks.empty())
+        CK(cudaMemcpyAsync(ctx->chunks, chunks.data(), sizeof(Chunk) * chunks.size(),
+                           cudaMemcpyHostToDevice, st));
+    // Box accumulators start empty.
+    CK(cudaMemsetAsync(ctx->bbox32, 0, 6ull * ctx->nsys * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(ctx->bbox64, 0, 6ull * ctx->nsys * sizeof(unsigned long long), st));
+    {
+        std::vector<uint32_t> lo32(6ull * ctx->nsys, 0);
+        std::vector<unsigned long long> lo64(6ull * ctx->nsys, 0);
+        for (uint32_t s = 0; s < ctx->nsys; ++s)
+            for (int a = 0; a < 3; ++a) {
+                lo32[6ull * s + a] = ~0u;
+                lo64[6ull * s + a] = ~0ull;
+            }
+        CK(cudaMemcpyAsync(ctx->bbox32, lo32.data(), lo32.size() * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->bbox64, lo64.data(), lo64.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // the host vectors go out of scope
+    }
+    // Particles through the staging buffer.
+    char* stg = static_cast<char*>(ctx->staging);
+    PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
+    VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);
+    CK(cudaMemcpyAsync(d_pm, pm, sizeof(PositionMass) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_vr, vr, sizeof(VelocityRadius) * n, cudaMemcpyHostToDevice, st));
+    ColorType* d_ct = nullptr;
+    if (ct) {
+        // ColorType shares the staging area after the velocities are converted.
+        CK(astro::launch_upload_convert(prec, d_pm, d_vr, nullptr, ctx->pos[0], ctx->vel[0],
+                                        phys ? ctx->ids[0] : nullptr, nullptr, ctx->x64[0], n,
+                                        n_tree, st));
+        d_ct = reinterpret_cast<ColorType*>(stg);
+        CK(cudaMemcpyAsync(d_ct, ct, sizeof(ColorType) * n, cudaMemcpyHostToDevice, st));
+        CK(astro::launch_types_from_colors(d_ct, ctx->types, n, st));
+    } else {
+        CK(astro::launch_upload_convert(prec, d_pm, d_vr, nullptr, ctx->pos[0], ctx->vel[0],
+                                        phys ? ctx->ids[0] : nullptr, ctx->types, ctx->x64[0], n,
+                                        n_tree, st));
+    }
+    ctx->uploaded = true;
+    return ASTRO_OK;
+}
+
+int astro_upload(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                 const ColorType* ct, uint32_t n, uint32_t n_tree) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!pm || !vr || n == 0 || n_tree > n)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload: null pointer, n == 0 or n_tree > n");
+    if (n > ctx->max_n) return fail(ctx, ASTRO_ERR_CAPACITY, "upload: n exceeds max_n");
+    if (is_phys(ctx) && n_tree != n)
+        return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "PHYSICAL preset needs n_tree == n");
+    std::vector<uint32_t> sizes(1, n_tree);
+    return upload_common(ctx, pm, vr, ct, n, n_tree, sizes);
+}
+
+int astro_upload_systems(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                         const uint32_t* sys_sizes, uint32_t nsys) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!pm || !vr || !sys_sizes || nsys == 0)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload_systems: null pointer or nsys == 0");
+    if (!is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "systems need the PHYSICAL preset");
+    if (nsys > ctx->max_sys) return fail(ctx, ASTRO_ERR_CAPACITY, "nsys exceeds max_systems");
+    uint64_t total = 0;
+    std::vector<uint32_t> sizes(sys_sizes, sys_sizes + nsys);
+    for (uint32_t s : sizes) {
+        if (s == 0) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "empty system");
+        total += s;
+    }
+    if (total > ctx->max_n) return fail(ctx, ASTRO_ERR_CAPACITY, "total particles exceed max_n");
+    return upload_common(ctx, pm, vr, nullptr, (uint32_t)total, (uint32_t)total, sizes);
+}
+
+int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!ctx->uploaded) return fail(ctx, ASTRO_ERR_STATE, "download before upload");
+    if (n != ctx->n || (!pm && !vr)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "download: n mismatch");
+    cudaStream_t st = ctx->stream;
+    const Cur c = current(ctx);
+    char* stg = static_cast<char*>(ctx->staging);
+    PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
+    VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);
+    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st));
+    if (pm) CK(cudaMemcpyAsync(pm, d_pm, sizeof(PositionMass) * n, cudaMemcpyDeviceToHost, st));
+    if (vr) CK(cudaMemcpyAsync(vr, d_vr, sizeof(VelocityRadius) * n, cudaMemcpyDeviceToHost, st));
+    return check_device(ctx);
+}
+
+#define NEED_UPLOAD()                                                          \
+    do {                                                                       \
+        if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;                           \
+        if (!ctx->uploaded) return fail(ctx, ASTRO_ERR_STATE, "no upload yet"); \
+    } while (0)
+
+int astro_encode(astro_ctx* ctx) {
+    NEED_UPLOAD();
+    drop_graph(ctx);
+    return stage_encode(ctx);
+}
+int astro_sort(astro_ctx* ctx) {
+    NEED_UPLOAD();
+    drop_graph(ctx);
+    return stage_sort(ctx);
+}
+int astro_build(astro_ctx* ctx) {
+    NEED_UPLOAD();
+    drop_graph(ctx);
+    return stage_build(ctx);
+}
+int astro_traverse(astro_ctx* ctx) {
+    NEED_UPLOAD();
+    drop_graph(ctx);
+    return stage_traverse(ctx, 0.0f, false);
+}
+int astro_integrate(astro_ctx* ctx, float dt) {
+    NEED_UPLOAD();
+    drop_graph(ctx);
+    return stage_integrate(ctx, dt);
+}
+
+int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps) {
+    NEED_UPLOAD();
+    if (!std::isfinite(dt)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "dt must be finite");
+    if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "step called between sort and traverse");
+    const bool use_graph = (ctx->p.flags & ASTRO_FLAG_NO_GRAPH) == 0;
+    uint32_t done = 0;
+    int r;
+    if (use_graph && nsteps > 1 && !(ctx->graph_valid && ctx->graph_dt == dt)) {
+        // One eager step first (it also completes one-time set-up), then capture.
+        if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
+        done = 1;
+        if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
+    }
+    for (; done < nsteps; ++done) {
+        if (use_graph && ctx->graph_valid && ctx->graph_dt == dt) {
+            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+            ctx->tree_valid = true;
+        } else {
+            if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
+        }
+    }
+    return ASTRO_OK;
+}
+
+int astro_synchronize(astro_ctx* ctx) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    return check_device(ctx);
+}
+
+int astro_get_stream(astro_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return ASTRO_ERR_INVALID_ARGUMENT;
+    *stream = ctx->stream;
+    return ASTRO_OK;
+}
+
+int astro_read_keys(astro_ctx* ctx, uint64_t* codes, uint64_t* sorted_codes,
+                    uint32_t* sorted_indices, uint32_t n) {
+    NEED_UPLOAD();
+    const uint32_t count = is_phys(ctx) ? ctx->n : ctx->n_tree;
+    if (n != count) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_keys: n must be the tree count");
+    cudaStream_t st = ctx->stream;
+    const Cur c = current(ctx);
+    uint64_t* tmp = static_cast<uint64_t*>(ctx->staging);
+    if (codes) {
+        if (is_phys(ctx)) {
+            CK(astro::launch_scatter_u64(ctx->sorted_keys, c.ids, tmp, n, st));
+            CK(cudaMemcpyAsync(codes, tmp, 8ull * n, cudaMemcpyDeviceToHost, st));
+        } else {
+            CK(cudaMemcpyAsync(codes, ctx->codes, 8ull * n, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    if (sorted_codes)
+        CK(cudaMemcpyAsync(sorted_codes, ctx->sorted_keys, 8ull * n, cudaMemcpyDeviceToHost, st));
+    if (sorted_indices)
+        CK(cudaMemcpyAsync(sorted_indices, is_phys(ctx) ? c.ids : ctx->perm, 4ull * n,
+                           cudaMemcpyDeviceToHost, st));
+    if (codes) CK(cudaStreamSynchronize(st));
+    return check_device(ctx);
+}
+
+int astro_read_tree_info(astro_ctx* ctx, uint32_t* n_layers, uint32_t* layer_sizes,
+                         uint32_t* layer_offsets, uint32_t* layer_counts, uint32_t max_layers) {
+    NEED_UPLOAD();
+    const uint32_t L = ctx->layers.n_layers;
+    if (n_layers) *n_layers = L;
+    if ((layer_sizes || layer_offsets || layer_counts) && max_layers < L)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_tree_info: max_layers too small");
+    for (uint32_t l = 0; l < L; ++l) {
+        if (layer_sizes) layer_sizes[l] = ctx->layers.size[l];
+        if (layer_offsets) layer_offsets[l] = ctx->layers.offset[l];
+    }
+    if (layer_counts) {
+        CK(cudaMemcpyAsync(layer_counts, ctx->layer_count, 4ull * L, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    }
+    return check_device(ctx);
+}
+
+int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t count) {
+    NEED_UPLOAD();
+    if (!nodes || first + count > ctx->capacity)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_nodes: range outside the node capacity");
+    cudaStream_t st = ctx->stream;
+    const uint64_t chunk = 1ull << 18;  // nodes per staging round (32 MB)
+    if (!ctx->readback) {
+        ctx->readback_bytes = chunk * sizeof(OctreeNode);
+        CK(cudaMalloc(&ctx->readback, ctx->readback_bytes));
+    }
+    OctreeNode* d_out = static_cast<OctreeNode*>(ctx->readback);
+    uint64_t pos = first;
+    while (pos < first + count) {
+        // Layer of slot pos.
+        uint32_t l = 0;
+        while (l + 1 < ctx->layers.n_layers && ctx->layers.offset[l + 1] <= pos) ++l;
+        const uint64_t layer_end = (uint64_t)ctx->layers.offset[l] + ctx->layers.size[l];
+        const uint64_t m = std::min<uint64_t>({chunk, first + count - pos, layer_end - pos});
+        CK(astro::launch_readback_nodes(ctx->node_cm, ctx->node_rng, ctx->node_key,
+                                        ctx->layer_count, l, ctx->layers.offset[l],
+                                        (uint32_t)(pos - ctx->layers.offset[l]), (uint32_t)m, d_out,
+                                        st));
+        CK(cudaMemcpyAsync(nodes + (pos - first), d_out, m * sizeof(OctreeNode),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        pos += m;
+    }
+    return check_device(ctx);
+}
+
+int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n) {
+    NEED_UPLOAD();
+    if (!acc4 || n != ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_accel: n mismatch");
+    cudaStream_t st = ctx->stream;
+    if (is_phys(ctx)) {
+        float4* tmp = static_cast<float4*>(ctx->staging);
+        CK(astro::launch_scatter_f4(ctx->acc, current(ctx).ids, tmp, n, st));
+        CK(cudaMemcpyAsync(acc4, tmp, 16ull * n, cudaMemcpyDeviceToHost, st));
+    } else {
+        CK(cudaMemcpyAsync(acc4, ctx->acc, 16ull * n, cudaMemcpyDeviceToHost, st));
+    }
+    return check_device(ctx);
+}
+
+int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits) {
+    NEED_UPLOAD();
+    unsigned long long s[2] = {0, 0};
+    CK(cudaMemcpyAsync(s, ctx->stats, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
+    int r = check_device(ctx);
+    if (interactions) *interactions = s[0];
+    if (node_visits) *node_visits = s[1];
+    return r;
+}
+
+int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t n_sample,
+                           double* acc3) {
+    NEED_UPLOAD();
+    if (!sample_idx || !acc3 || n_sample == 0 || n_sample > ctx->n)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "direct_accel: bad samples");
+    if (!is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "direct sum needs the PHYSICAL preset");
+    cudaStream_t st = ctx->stream;
+    const Cur c = current(ctx);
+    // Staging layout: inverse ids | samples | slots | begin | end | out.
+    char* stg = static_cast<char*>(ctx->staging);
+    uint32_t* inv = reinterpret_cast<uint32_t*>(stg);
+    uint32_t* d_samples = inv + ctx->n;
+    uint32_t* d_slots = d_samples + n_sample;
+    uint32_t* d_begin = d_slots + n_sample;
+    uint32_t* d_end = d_begin + n_sample;
+    double* d_out = reinterpret_cast<double*>(
+        (reinterpret_cast<uintptr_t>(d_end + n_sample) + 15) & ~uintptr_t(15));
+    std::vector<uint32_t> begin(n_sample), end(n_sample);
+    std::vector<uint32_t> offs(ctx->sys_sizes.size() + 1, 0);
+    for (size_t s = 0; s < ctx->sys_sizes.size(); ++s) offs[s + 1] = offs[s] + ctx->sys_sizes[s];
+    for (uint32_t k = 0; k < n_sample; ++k) {
+        if (sample_idx[k] >= ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "sample out of range");
+        const size_t s = std::upper_bound(offs.begin(), offs.end(), sample_idx[k]) - offs.begin() - 1;
+        begin[k] = offs[s];
+        end[k] = offs[s + 1];
+    }
+    CK(astro::launch_inverse_ids(c.ids, inv, ctx->n, st));
+    CK(cudaMemcpyAsync(d_samples, sample_idx, 4ull * n_sample, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_begin, begin.data(), 4ull * n_sample, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_end, end.data(), 4ull * n_sample, cudaMemcpyHostToDevice, st));
+    CK(astro::launch_gather_u32(inv, d_samples, d_slots, n_sample, st));
+    astro::DirectArgs a{};
+    a.pos = c.pos;
+    a.x64 = is_prec(ctx) ? c.x64 : nullptr;
+    a.slot = d_slots;
+    a.sys_begin = d_begin;
+    a.sys_end = d_end;
+    a.out = d_out;
+    a.n = ctx->n;
+    a.n_sample = n_sample;
+    a.g = ctx->p.g;
+    a.eps2 = (double)ctx->p.softening * (double)ctx->p.softening;
+    CK(astro::launch_direct_sum(a, st));
+    CK(cudaMemcpyAsync(acc3, d_out, 24ull * n_sample, cudaMemcpyDeviceToHost, st));
+    return check_device(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// Internal declarations shared by the translation units of libastro_cuda.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/astro_cuda.h"
+
+namespace astro {
+
+// Per-system quantiser, frame and opening thresholds, rebuilt every step by
+// the setup kernel from the bounding box of the current positions.
+struct SysInfo {
+    float lo[3];       // lower corner of the box, in the system's FP32 frame
+    float scale;       // 2^21 / extent
+    float ext;         // box extent (largest axis)
+    uint32_t root;     // node index of the system's root
+    uint32_t begin;    // particle range (the same in upload and Morton order)
+    uint32_t end;
+    double origin[3];  // precision form: FP64 origin of the FP32 frame
+    double _pad0;
+    float crit2[ASTRO_MAX_LAYERS];  // (cell size / theta)^2 per layer
+    uint32_t _pad1[2];
+};
+
+// Contiguous particle range inside one system, processed by one block of the
+// per-particle kernels that need to know the system (bbox, encode).
+struct Chunk {
+    uint32_t sys, begin, end, _pad;
+};
+constexpr uint32_t kChunkParticles = 4096;
+
+struct LayerTable {
+    uint32_t n_layers;
+    uint32_t offset[ASTRO_MAX_LAYERS];
+    uint32_t size[ASTRO_MAX_LAYERS];
+};
+
+// ---------------------------------------------------------------- sort ----
+struct SortPlan {
+    size_t keys_tmp, vals_tmp, excl, zero_begin, hist, counters, lookback, zero_end, total;
+    uint32_t passes, ntiles, tile;
+};
+SortPlan sort_plan(uint32_t max_len, uint32_t key_bits);
+// Stable sort of n_est (key, value) pairs (count read from d_count when not
+// NULL). vals_in NULL => values are 0..n-1. err (device word) collects
+// look-back timeouts; NULL => the word inside temp.
+cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                       uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
+                       uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
+                       uint32_t* err);
+
+// ------------------------------------------------------------ pipeline ----
+struct DeviceState;  // defined in context.cu
+
+}  // namespace astro
+
+// The opaque context of the C ABI.
+struct astro_ctx {
+    astro_params p{};
+    uint32_t max_n = 0, max_sys = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    // Current upload.
+    bool uploaded = false;
+    uint32_t n = 0, n_tree = 0, nsys = 0;
+    uint32_t lbits = 6, sysbits = 0, key_bits = 18;
+    astro::LayerTable layers{};
+    uint64_t capacity = 0;
+    uint32_t nchunks = 0;
+    bool tree_valid = false;
+    bool state_in_b = false;          // PHYSICAL: current state in the B buffers
+    std::vector<uint32_t> sys_sizes;
+
+    // Particle state. PHYSICAL keeps it in Morton order (buffer A holds the
+    // current state between steps; B is the permuted copy within a step).
+    float4* pos[2] = {nullptr, nullptr};
+    float4* vel[2] = {nullptr, nullptr};
+    uint32_t* ids[2] = {nullptr, nullptr};
+    double* x64[2] = {nullptr, nullptr};  // SoA x | y | z, precision form
+    float4* acc = nullptr;
+    uint32_t* types = nullptr;
+    uint64_t* codes = nullptr;        // keys in the state order before sorting
+    uint64_t* sorted_keys = nullptr;
+    uint32_t* perm = nullptr;
+    void* staging = nullptr;          // upload/download, 64 B per particle
+    size_t staging_bytes = 0;
+
+    // Tree.
+    uint64_t tree_capacity = 0;       // allocated node slots
+    float4* node_cm = nullptr;        // centre of mass, mass
+    uint4* node_rng = nullptr;        // first child, end child, first particle, end particle
+    uint64_t* node_key = nullptr;
+    void* node_sum = nullptr;         // float4 or double4 raw sums (S, M)
+    uint32_t* node_pbeg = nullptr;
+    uint32_t* node_cbeg = nullptr;
+    uint32_t* layer_count = nullptr;  // device [ASTRO_MAX_LAYERS]
+
+    // Systems.
+    astro::SysInfo* sys = nullptr;
+    uint32_t* bbox32 = nullptr;               // 6 per system
+    unsigned long long* bbox64 = nullptr;     // 6 per system
+    astro::Chunk* chunks = nullptr;
+    uint32_t chunk_capacity = 0;
+
+    // Scratch.
+    void* sort_temp = nullptr;
+    size_t sort_temp_bytes = 0;
+    uint32_t* topo_lookback = nullptr;
+    size_t topo_lookback_words = 0;
+    uint32_t* counters = nullptr;             // [0] topology tiles, [1] traversal queue
+    uint32_t* err = nullptr;                  // device error word
+    unsigned long long* stats = nullptr;      // interactions, node visits
+    void* readback = nullptr;
+    size_t readback_bytes = 0;
+
+    // Graph of one step.
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.0f;
+    bool graph_valid = false;
+
+    std::string last_error;
+};

@@ -1,0 +1,333 @@
+// Onesweep LSD radix sort of (uint64 key, uint32 value) pairs for sm_103a.
+//
+// Replaces MetalKernelsRadixSort.sort (Astro/RadixSort.swift:98-185), whose
+// 64 one-bit split passes (split_prep / prefixSum / prefixFixup /
+// split_scatter, Astro/RadixSort.metal:30-131) each move the whole key and
+// index arrays. Here the key is consumed 8 bits per pass:
+//   1. one histogram kernel reads the keys once and counts every digit of
+//      every pass (warp-ballot peer groups, shared-memory histograms); its
+//      last block turns the counts into exclusive digit offsets;
+//   2. one kernel per pass: each block takes the next tile (atomic ticket),
+//      ranks its keys stably with warp-ballot peer masks and per-warp digit
+//      counters in shared memory, publishes its digit counts, obtains the
+//      counts of all earlier tiles by decoupled look-back (bounded waits),
+//      and scatters through shared memory so that runs of one digit leave
+//      as contiguous stores.
+// A stable LSD sort yields the one stable permutation, so the result equals
+// the reference's bit by bit, including the order of equal keys.
+#include "common.cuh"
+#include "internal.h"
+
+namespace astro {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // 4096 pairs per tile
+constexpr int kRadix = 256;
+constexpr int kMaxPasses = 8;
+constexpr int kHistBlocksPerSm = 4;
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kWarps ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < kWarps; o <<= 1) {
+            uint32_t y = __shfl_up_sync(kFullMask, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        if (lane < kWarps) s_warp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t r = (warp ? s_warp[warp - 1] : 0u) + x - v;
+    __syncthreads();
+    return r;
+}
+
+// Lanes of the warp whose digit equals this lane's digit, among `valid`.
+__device__ __forceinline__ uint32_t peer_mask(uint32_t digit, uint32_t bits, uint32_t valid) {
+    uint32_t peers = valid;
+    for (uint32_t b = 0; b < bits; ++b) {
+        uint32_t bit = (digit >> b) & 1u;
+        uint32_t ballot = __ballot_sync(kFullMask, bit);
+        peers &= bit ? ballot : ~ballot;
+    }
+    return peers;
+}
+
+__global__ __launch_bounds__(kThreads) void sort_histogram_kernel(
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ d_count, uint32_t n_est,
+    uint32_t key_bits, uint32_t passes, uint32_t* __restrict__ hist, uint32_t* __restrict__ excl,
+    uint32_t* __restrict__ done) {
+    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    __shared__ uint32_t s_warp[kWarps];
+    __shared__ bool s_last;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t n = d_count ? min(*d_count, n_est) : n_est;
+    for (uint32_t i = tid; i < passes * kRadix; i += kThreads) s_hist[i] = 0;
+    __syncthreads();
+    const uint32_t lt = lanemask_lt();
+    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads; base < n; base += stride) {
+        const uint64_t i = base + tid;
+        const bool valid = i < n;
+        const uint64_t key = valid ? __ldcs(keys + i) : 0ull;
+        const uint32_t vmask = __ballot_sync(kFullMask, valid);
+        for (uint32_t p = 0; p < passes; ++p) {
+            const uint32_t shift = 8u * p;
+            const uint32_t bits = min(8u, key_bits - shift);
+            const uint32_t digit = (uint32_t)(key >> shift) & ((1u << bits) - 1u);
+            const uint32_t peers = peer_mask(digit, bits, vmask);
+            if (valid && (peers & lt) == 0) atomicAdd(&s_hist[p * kRadix + digit], __popc(peers));
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < passes * kRadix; i += kThreads)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint32_t c = __ldcg(&hist[p * kRadix + tid]);
+        excl[p * kRadix + tid] = block_exclusive_scan(c, s_warp);
+    }
+}
+
+struct PassSmem {
+    union {
+        uint32_t warp_hist[kWarps][kRadix];  // ranking: per-warp digit counters
+        struct {
+            uint64_t keys[kTile];
+            uint32_t vals[kTile];
+        } stage;                             // scatter: the tile in sorted order
+    } u;
+    uint32_t tile_start[kRadix];   // first slot of each digit inside the tile
+    uint32_t global_base[kRadix];  // first output slot of each digit of this tile
+    uint32_t scan_tmp[kWarps];
+    uint32_t tile_id;
+};
+
+__global__ __launch_bounds__(kThreads, 2) void sort_pass_kernel(
+    const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+    uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+    const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
+    uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
+    uint32_t digit_bits, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PassSmem& sm = *reinterpret_cast<PassSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = d_count ? min(*d_count, n_est) : n_est;
+    if (tid == 0) sm.tile_id = atomicAdd(tile_counter, 1u);
+    for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&sm.u.warp_hist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = sm.tile_id;
+    const uint64_t tile_base = (uint64_t)tile * kTile;
+    if (tile_base >= n) return;
+    const uint32_t dmask = (1u << digit_bits) - 1u;
+    const uint32_t lt = lanemask_lt();
+
+    // Warp-striped load: warp w owns a contiguous 32*kItems slice, item k of
+    // lane j sits at slice + 32k + j, so processing k in order keeps the
+    // ranking stable.
+    uint64_t key[kItems];
+    uint32_t val[kItems], pos[kItems];
+    const uint64_t warp_base = tile_base + (uint64_t)warp * 32 * kItems;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i = warp_base + 32ull * k + lane;
+        const bool valid = i < n;
+        key[k] = valid ? __ldcs(keys_in + i) : ~0ull;
+        val[k] = valid ? (vals_in ? __ldcs(vals_in + i) : (uint32_t)i) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i = warp_base + 32ull * k + lane;
+        const bool valid = i < n;
+        const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
+        const uint32_t peers = peer_mask(digit, digit_bits, __ballot_sync(kFullMask, valid));
+        const uint32_t lower = __popc(peers & lt), cnt = __popc(peers);
+        uint32_t old = 0;
+        if (valid) old = sm.u.warp_hist[warp][digit];
+        __syncwarp();
+        if (valid && lower + 1 == cnt) sm.u.warp_hist[warp][digit] = old + cnt;
+        __syncwarp();
+        pos[k] = old + lower;
+    }
+    __syncthreads();
+
+    // Thread d owns digit d: per-warp exclusive offsets and the tile count.
+    uint32_t tile_cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        uint32_t c = sm.u.warp_hist[w][tid];
+        sm.u.warp_hist[w][tid] = tile_cnt;
+        tile_cnt += c;
+    }
+    uint32_t* my_word = lookback + (size_t)tile * kRadix + tid;
+    st_relaxed_u32(my_word, (tile == 0 ? kLbInclusive : kLbAggregate) | tile_cnt);
+    const uint32_t tile_start = block_exclusive_scan(tile_cnt, sm.scan_tmp);
+    sm.tile_start[tid] = tile_start;
+    uint32_t prefix = 0;
+    if (tile > 0) {
+        for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
+            const uint32_t v = lookback_wait(lookback + (size_t)j * kRadix + tid, err);
+            prefix += v & kLbCountMask;
+            if ((v & kLbInclusive) != 0) break;
+        }
+        st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
+    }
+    sm.global_base[tid] = excl[tid] + prefix;
+    __syncthreads();
+
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
+        pos[k] += sm.tile_start[digit] + sm.u.warp_hist[warp][digit];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i = warp_base + 32ull * k + lane;
+        if (i < n) {
+            sm.u.stage.keys[pos[k]] = key[k];
+            sm.u.stage.vals[pos[k]] = val[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = (uint32_t)min((uint64_t)kTile, (uint64_t)n - tile_base);
+    for (uint32_t i = tid; i < tile_n; i += kThreads) {
+        const uint64_t k = sm.u.stage.keys[i];
+        const uint32_t digit = (uint32_t)(k >> shift) & dmask;
+        const uint32_t o = sm.global_base[digit] + (i - sm.tile_start[digit]);
+        keys_out[o] = k;
+        vals_out[o] = sm.u.stage.vals[i];
+    }
+}
+
+int g_num_sms = 0;
+
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+}  // namespace
+
+SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
+    SortPlan p{};
+    p.passes = key_bits == 0 ? 1u : (key_bits + 7u) / 8u;
+    p.tile = kTile;
+    p.ntiles = (uint32_t)(((uint64_t)max_len + kTile - 1) / kTile);
+    size_t off = 0;
+    p.keys_tmp = off;
+    off = align_up(off + 8ull * max_len, 256);
+    p.vals_tmp = off;
+    off = align_up(off + 4ull * max_len, 256);
+    p.excl = off;
+    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
+    p.zero_begin = off;
+    p.hist = off;
+    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
+    p.counters = off;  // [0..7] tile tickets per pass, [8] histogram blocks done, [9] error
+    off = align_up(off + 4ull * 16, 256);
+    p.lookback = off;
+    off = align_up(off + 4ull * p.passes * (size_t)std::max(p.ntiles, 1u) * kRadix, 256);
+    p.zero_end = off;
+    p.total = off;
+    return p;
+}
+
+cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                       uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
+                       uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
+                       uint32_t* err) {
+    if (n_est == 0) return cudaSuccess;
+    const SortPlan plan = sort_plan(n_est, key_bits);
+    if (temp_bytes < plan.total || key_bits > 64) return cudaErrorInvalidValue;
+    static bool attr_set = false;
+    const size_t smem = sizeof(PassSmem);
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    char* base = static_cast<char*>(temp);
+    uint64_t* keys_tmp = reinterpret_cast<uint64_t*>(base + plan.keys_tmp);
+    uint32_t* vals_tmp = reinterpret_cast<uint32_t*>(base + plan.vals_tmp);
+    uint32_t* excl = reinterpret_cast<uint32_t*>(base + plan.excl);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base + plan.hist);
+    uint32_t* counters = reinterpret_cast<uint32_t*>(base + plan.counters);
+    uint32_t* lookback = reinterpret_cast<uint32_t*>(base + plan.lookback);
+    if (!err) err = counters + 9;
+    cudaError_t e = cudaMemsetAsync(base + plan.zero_begin, 0, plan.zero_end - plan.zero_begin, st);
+    if (e != cudaSuccess) return e;
+    const uint32_t hist_blocks = (uint32_t)std::min<uint64_t>(
+        ((uint64_t)n_est + kThreads - 1) / kThreads, (uint64_t)num_sms() * kHistBlocksPerSm);
+    sort_histogram_kernel<<<hist_blocks, kThreads, 0, st>>>(keys_in, d_count, n_est, key_bits,
+                                                            plan.passes, hist, excl, counters + 8);
+    const uint64_t* kin = keys_in;
+    const uint32_t* vin = vals_in;
+    for (uint32_t p = 0; p < plan.passes; ++p) {
+        const bool to_out = ((plan.passes - 1 - p) % 2) == 0;
+        uint64_t* kout = to_out ? keys_out : keys_tmp;
+        uint32_t* vout = to_out ? vals_out : vals_tmp;
+        const uint32_t shift = 8u * p;
+        const uint32_t bits = key_bits == 0 ? 0u : std::min(8u, key_bits - shift);
+        sort_pass_kernel<<<plan.ntiles, kThreads, smem, st>>>(
+            kin, vin, kout, vout, d_count, n_est, excl + p * kRadix,
+            lookback + (size_t)p * plan.ntiles * kRadix, counters + p, shift, bits, err);
+        kin = kout;
+        vin = vout;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace astro
+
+extern "C" int astro_radix_sort_temp_bytes(uint32_t max_length, uint32_t key_bits, size_t* bytes) {
+    if (!bytes || key_bits > 64) return ASTRO_ERR_INVALID_ARGUMENT;
+    *bytes = astro::sort_plan(max_length, key_bits).total;
+    return ASTRO_OK;
+}
+
+// MetalKernelsRadixSort.sort (Astro/RadixSort.swift:98-105): input/inputIndices
+// are read, output/outputIndices receive the sorted pairs, estimatedLength
+// sizes the launch and actualCountBuffer (d_actual_count) holds the count.
+extern "C" int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
+                                uint64_t* d_output, uint32_t* d_output_indices,
+                                uint32_t estimated_length, const uint32_t* d_actual_count,
+                                uint32_t key_bits, void* d_temp, size_t temp_bytes, void* stream) {
+    if (estimated_length == 0) return ASTRO_OK;  // RadixSort.swift:106
+    if (!d_input || !d_output || !d_output_indices || !d_temp || key_bits > 64)
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    if ((const void*)d_input == (const void*)d_output ||
+        (const void*)d_input_indices == (const void*)d_output_indices)
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    if (temp_bytes < astro::sort_plan(estimated_length, key_bits).total) return ASTRO_ERR_CAPACITY;
+    cudaError_t e = astro::sort_pairs(d_input, d_input_indices, d_output, d_output_indices,
+                                      estimated_length, d_actual_count, key_bits, d_temp,
+                                      temp_bytes, static_cast<cudaStream_t>(stream), nullptr);
+    return e == cudaSuccess ? ASTRO_OK : ASTRO_ERR_CUDA;
+}

@@ -1,0 +1,93 @@
+"""Byte layouts of include/astro_cuda.h as numpy dtypes and ctypes structures.
+
+The particle and node records keep the reference's layouts (Astro/bridge.h:
+17-65): Metal's float3 occupies 16 bytes, so PositionMass, VelocityRadius and
+ColorType are 32-byte records and OctreeNode is a 128-byte record.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+INVALID_MORTON_CODE = 0xFFFFFFFFFFFFFFFF  # bridge.h:91-94
+INVALID_CHILD = 0xFFFFFFFF  # Octree.metal:10
+MAX_LBITS = 21
+MAX_LAYERS = MAX_LBITS + 1
+
+PRESET_REFERENCE = 0
+PRESET_PHYSICAL = 1
+FORM_PLAIN = 0
+FORM_PRECISION = 1
+FLAG_IEEE_EXACT = 0x1
+FLAG_NO_GRAPH = 0x2
+FLAG_PERSISTENT = 0x4
+
+IC_PLUMMER = 0
+IC_DISK_BULGE = 1
+IC_TWO_PLUMMER = 2
+IC_UNIFORM_CUBE = 3
+IC_REFERENCE_SCENE = 4
+
+POSITION_MASS = np.dtype([("position", "<f4", (3,)), ("_pad0", "<f4"), ("mass", "<f4"),
+                          ("_pad1", "<f4", (3,))], align=False)
+VELOCITY_RADIUS = np.dtype([("velocity", "<f4", (3,)), ("_pad0", "<f4"), ("radius", "<f4"),
+                            ("_pad1", "<f4", (3,))], align=False)
+COLOR_TYPE = np.dtype([("color", "<f4", (4,)), ("type", "<u4"), ("_pad", "<u4", (3,))],
+                      align=False)
+OCTREE_NODE = np.dtype([
+    ("mortonCode", "<u8"), ("_pad0", "<u8"),
+    ("centerOfMass", "<f4", (3,)), ("_pad1", "<f4"),
+    ("totalMass", "<f4"), ("_pad2", "<f4", (3,)),
+    ("emittedColor", "<f4", (4,)),
+    ("emittedColorCenter", "<f4", (3,)), ("_pad3", "<f4"),
+    ("children", "<u4", (8,)),
+    ("layer", "<u4"), ("_pad4", "<u4", (3,)),
+], align=False)
+
+assert POSITION_MASS.itemsize == 32 and VELOCITY_RADIUS.itemsize == 32
+assert COLOR_TYPE.itemsize == 32 and OCTREE_NODE.itemsize == 128
+assert OCTREE_NODE.fields["totalMass"][1] == 32 and OCTREE_NODE.fields["children"][1] == 80
+assert OCTREE_NODE.fields["layer"][1] == 112
+
+
+class Params(ctypes.Structure):
+    """astro_params: every constant the reference hard-codes."""
+
+    _fields_ = [
+        ("preset", ctypes.c_uint32),
+        ("form", ctypes.c_uint32),
+        ("lbits", ctypes.c_uint32),
+        ("flags", ctypes.c_uint32),
+        ("theta", ctypes.c_float),
+        ("g", ctypes.c_float),
+        ("softening", ctypes.c_float),
+        ("leaf_min_dist2", ctypes.c_float),
+        ("force_clamp", ctypes.c_float),
+        ("quant_offset", ctypes.c_float),
+        ("damping", ctypes.c_float),
+        ("type_accel_scale", ctypes.c_float * 3),
+        ("bucket", ctypes.c_uint32),
+        ("block_warps", ctypes.c_uint32),
+        ("_reserved", ctypes.c_uint32 * 6),
+    ]
+
+    def replace(self, **kw) -> "Params":
+        out = Params()
+        ctypes.pointer(out)[0] = self
+        for k, v in kw.items():
+            if k == "type_accel_scale":
+                out.type_accel_scale = (ctypes.c_float * 3)(*v)
+            else:
+                setattr(out, k, v)
+        return out
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("_")}
+        d["type_accel_scale"] = list(self.type_accel_scale)
+        return d
+
+
+def empty_particles(n: int):
+    """Zeroed PositionMass and VelocityRadius arrays of length n."""
+    return np.zeros(n, POSITION_MASS), np.zeros(n, VELOCITY_RADIUS)

@@ -1,0 +1,174 @@
+"""Host-side mirror of the reference's per-frame compute (Renderer).
+
+``Simulation`` owns one libastro_cuda context. Its methods follow the
+reference's Renderer (Astro/Renderer.swift): ``make_buffers`` /
+``make_spheres`` become the constructor and ``upload``, ``draw`` runs the
+compute section of a frame, and the stage methods ``generate_morton_codes``,
+``sort``, ``build_tree``, ``barnes_hut`` and ``update_spheres`` run one stage
+each, in the reference's order (Renderer.swift:505-542).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+from . import layouts as L
+from ._native import check, lib, ptr
+
+
+def default_params(preset: int = L.PRESET_PHYSICAL, **overrides) -> L.Params:
+    p = L.Params()
+    check(lib().astro_params_default(preset, byref(p)))
+    return p.replace(**overrides) if overrides else p
+
+
+class Simulation:
+    """One Barnes-Hut context on the current CUDA device."""
+
+    def __init__(self, params: L.Params | None = None, max_n: int = 1 << 20,
+                 max_systems: int = 1):
+        self.params = params if params is not None else default_params()
+        h = c_void_p()
+        check(lib().astro_create(byref(self.params), max_n, max_systems, byref(h)))
+        self._h = h
+        self.max_n = max_n
+        self.n = 0
+        self.n_tree = 0
+        self.sys_sizes: list[int] = []
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            lib().astro_destroy(self._h)
+            self._h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, status: int) -> None:
+        check(status, self._h)
+
+    # -- parameters -------------------------------------------------------
+    def set_params(self, params: L.Params) -> None:
+        self._check(lib().astro_set_params(self._h, byref(params)))
+        self.params = params
+
+    # -- state ------------------------------------------------------------
+    def upload(self, pm: np.ndarray, vr: np.ndarray, ct: np.ndarray | None = None,
+               n_tree: int | None = None) -> None:
+        """Copy one system in (Renderer.makeSpheres' buffer copy)."""
+        pm = np.ascontiguousarray(pm, dtype=L.POSITION_MASS)
+        vr = np.ascontiguousarray(vr, dtype=L.VELOCITY_RADIUS)
+        n = len(pm)
+        n_tree = n if n_tree is None else n_tree
+        if ct is not None:
+            ct = np.ascontiguousarray(ct, dtype=L.COLOR_TYPE)
+        self._check(lib().astro_upload(self._h, ptr(pm), ptr(vr), ptr(ct), n, n_tree))
+        self.n, self.n_tree, self.sys_sizes = n, n_tree, [n_tree]
+
+    def upload_systems(self, pm: np.ndarray, vr: np.ndarray, sizes) -> None:
+        """Copy several independent systems in, laid out back to back."""
+        pm = np.ascontiguousarray(pm, dtype=L.POSITION_MASS)
+        vr = np.ascontiguousarray(vr, dtype=L.VELOCITY_RADIUS)
+        sz = np.ascontiguousarray(sizes, dtype=np.uint32)
+        arr = (c_uint32 * len(sz)).from_buffer(sz)
+        self._check(lib().astro_upload_systems(self._h, ptr(pm), ptr(vr), arr, len(sz)))
+        self.n = self.n_tree = int(sz.sum())
+        self.sys_sizes = [int(s) for s in sz]
+
+    def download(self, pm: np.ndarray | None = None, vr: np.ndarray | None = None):
+        pm = np.zeros(self.n, L.POSITION_MASS) if pm is None else pm
+        vr = np.zeros(self.n, L.VELOCITY_RADIUS) if vr is None else vr
+        self._check(lib().astro_download(self._h, ptr(pm), ptr(vr), self.n))
+        return pm, vr
+
+    # -- stages (Renderer.draw order) -------------------------------------
+    def generate_morton_codes(self) -> None:
+        self._check(lib().astro_encode(self._h))
+
+    def sort(self) -> None:
+        self._check(lib().astro_sort(self._h))
+
+    def build_tree(self) -> None:
+        self._check(lib().astro_build(self._h))
+
+    def barnes_hut(self) -> None:
+        self._check(lib().astro_traverse(self._h))
+
+    def update_spheres(self, dt: float) -> None:
+        self._check(lib().astro_integrate(self._h, dt))
+
+    def draw(self, dt: float, steps: int = 1) -> None:
+        """Run `steps` full steps (graph-replayed unless FLAG_NO_GRAPH)."""
+        self._check(lib().astro_step(self._h, dt, steps))
+
+    def synchronize(self) -> None:
+        self._check(lib().astro_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        s = c_void_p()
+        self._check(lib().astro_get_stream(self._h, byref(s)))
+        return s.value or 0
+
+    # -- readbacks --------------------------------------------------------
+    def read_keys(self):
+        n = self.n_tree
+        codes = np.zeros(n, np.uint64)
+        sorted_codes = np.zeros(n, np.uint64)
+        idx = np.zeros(n, np.uint32)
+        self._check(lib().astro_read_keys(self._h, ptr(codes), ptr(sorted_codes), ptr(idx), n))
+        return codes, sorted_codes, idx
+
+    def tree_info(self):
+        nl = c_uint32()
+        sizes = np.zeros(L.MAX_LAYERS, np.uint32)
+        offsets = np.zeros(L.MAX_LAYERS, np.uint32)
+        counts = np.zeros(L.MAX_LAYERS, np.uint32)
+        self._check(lib().astro_read_tree_info(self._h, byref(nl), ptr(sizes), ptr(offsets),
+                                               ptr(counts), L.MAX_LAYERS))
+        k = nl.value
+        return sizes[:k].copy(), offsets[:k].copy(), counts[:k].copy()
+
+    def read_nodes(self, first: int = 0, count: int | None = None) -> np.ndarray:
+        sizes, offsets, _ = self.tree_info()
+        cap = int(offsets[-1]) + int(sizes[-1])
+        count = cap - first if count is None else count
+        out = np.zeros(count, L.OCTREE_NODE)
+        self._check(lib().astro_read_nodes(self._h, ptr(out), first, count))
+        return out
+
+    def read_accel(self) -> np.ndarray:
+        out = np.zeros((self.n, 4), np.float32)
+        self._check(lib().astro_read_accel(self._h, ptr(out), self.n))
+        return out
+
+    def read_stats(self):
+        i, v = c_uint64(), c_uint64()
+        self._check(lib().astro_read_stats(self._h, byref(i), byref(v)))
+        return i.value, v.value
+
+    def direct_accel_f64(self, samples) -> np.ndarray:
+        s = np.ascontiguousarray(samples, dtype=np.uint32)
+        out = np.zeros((len(s), 3), np.float64)
+        self._check(lib().astro_direct_accel_f64(self._h, ptr(s), len(s), ptr(out)))
+        return out
+
+
+def version() -> str:
+    return lib().astro_version().decode()
+
+
+__all__ = ["Simulation", "default_params", "version"]
+_ = ctypes

@@ -1,0 +1,284 @@
+/*
+ * astro_cuda.h — C ABI of libastro_cuda, the sm_103a Barnes-Hut step.
+ *
+ * This header replaces three things in the osbo/astro reference:
+ *   1. the shared layouts of Astro/bridge.h (PositionMass, VelocityRadius,
+ *      ColorType, OctreeNode, INVALID_MORTON_CODE) — same byte layouts;
+ *   2. the Metal kernel entry points of the per-frame compute section of
+ *      Renderer.draw (Astro/Renderer.swift:495-542) — generateMortonCodes,
+ *      the radix sort, the layered octree build, barnesHut and updateSpheres;
+ *   3. the sort library MetalKernelsRadixSort.sort (Astro/RadixSort.swift:98-105).
+ *
+ * Conventions:
+ *   - Every function returns int: ASTRO_OK (0) or a negative astro_status.
+ *     Nothing aborts; the message of the last failure on a context is
+ *     available from astro_last_error().
+ *   - A context owns all of its device buffers and one CUDA stream. All work
+ *     is ordered on that stream. Only astro_download, astro_read_* and
+ *     astro_synchronize wait for the device.
+ *   - A context is not thread-safe; separate contexts are independent.
+ *   - Pointers named d_* are device pointers; all others are host pointers.
+ */
+#ifndef ASTRO_CUDA_H
+#define ASTRO_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASTRO_ABI_VERSION 1
+
+/* bridge.h:91-94 */
+#define ASTRO_INVALID_MORTON_CODE 0xFFFFFFFFFFFFFFFFull
+/* Octree.metal:10, BarnesHut.metal:7 */
+#define ASTRO_INVALID_CHILD 0xFFFFFFFFu
+/* 21 bits per axis fit a 63-bit key (MortonCode.metal:7-23). */
+#define ASTRO_MAX_LBITS 21
+#define ASTRO_MAX_LAYERS (ASTRO_MAX_LBITS + 1)
+/* Largest number of independent systems in one batched context. */
+#define ASTRO_MAX_SYSTEMS 65536
+
+#if defined(__GNUC__) || defined(__clang__)
+#define ASTRO_ALIGN16 __attribute__((aligned(16)))
+#else
+#define ASTRO_ALIGN16
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Shared layouts. Metal's float3 is 16 bytes with 16-byte alignment, so every
+ * float3 below is three floats plus one pad float.
+ * ------------------------------------------------------------------------- */
+
+/* bridge.h:17-24 — 32-byte stride: position @0, mass @16. */
+typedef struct ASTRO_ALIGN16 PositionMass {
+    float position[3];
+    float _pad0;
+    float mass;
+    float _pad1[3];
+} PositionMass;
+
+/* bridge.h:26-33 — 32-byte stride: velocity @0, radius @16. */
+typedef struct ASTRO_ALIGN16 VelocityRadius {
+    float velocity[3];
+    float _pad0;
+    float radius;
+    float _pad1[3];
+} VelocityRadius;
+
+/* bridge.h:35-43 — 32-byte stride: color @0, type @16.
+ * type 0 = star, 1 = planet, 2 = dust (Renderer.swift:448-472). */
+typedef struct ASTRO_ALIGN16 ColorType {
+    float color[4];
+    uint32_t type;
+    uint32_t _pad[3];
+} ColorType;
+
+/* bridge.h:47-65 — 128-byte node. emittedColor / emittedColorCenter are kept
+ * for layout compatibility; no kernel on the step reads them. */
+typedef struct ASTRO_ALIGN16 OctreeNode {
+    uint64_t mortonCode;        /* @0   */
+    uint64_t _pad0;             /* @8   */
+    float centerOfMass[3];      /* @16  */
+    float _pad1;                /* @28  */
+    float totalMass;            /* @32  */
+    float _pad2[3];             /* @36  */
+    float emittedColor[4];      /* @48  */
+    float emittedColorCenter[3];/* @64  */
+    float _pad3;                /* @76  */
+    uint32_t children[8];       /* @80  */
+    uint32_t layer;             /* @112 */
+    uint32_t _pad4[3];          /* @116 */
+} OctreeNode;
+
+/* ---------------------------------------------------------------------------
+ * Status codes.
+ * ------------------------------------------------------------------------- */
+typedef enum astro_status {
+    ASTRO_OK = 0,
+    ASTRO_ERR_INVALID_ARGUMENT = -1,
+    ASTRO_ERR_CAPACITY = -2,      /* n or the number of systems exceeds the context */
+    ASTRO_ERR_CUDA = -3,          /* a CUDA runtime call failed */
+    ASTRO_ERR_OUT_OF_MEMORY = -4,
+    ASTRO_ERR_STATE = -5,         /* call order violated (e.g. step before upload) */
+    ASTRO_ERR_DEVICE_TIMEOUT = -6,/* a bounded device-side wait gave up */
+    ASTRO_ERR_NOT_SUPPORTED = -7,
+    ASTRO_ERR_DEVICE_OVERFLOW = -8/* a device-side bound (stack depth) was hit */
+} astro_status;
+
+/* ---------------------------------------------------------------------------
+ * Parameters. Every constant the reference hard-codes is a field here.
+ * ------------------------------------------------------------------------- */
+typedef enum astro_preset {
+    /* The reference's literal semantics: (u32)(p + 1e6) quantiser,
+     * node size 2^(21+layer), monopole leaves with the self-leaf skip and the
+     * r^2 > 50 cut, g = 1e11, softening added to r^2, damped kick-drift with
+     * per-type multipliers, and the last-leaf range of aggregateLeafNodes. */
+    ASTRO_PRESET_REFERENCE = 0,
+    /* Physical units: bounding-box quantiser, geometric cell size, G and
+     * Plummer softening eps^2, particle-particle interaction inside opened
+     * leaves and buckets, leapfrog kick-drift-kick. */
+    ASTRO_PRESET_PHYSICAL = 1
+} astro_preset;
+
+typedef enum astro_form {
+    ASTRO_FORM_PLAIN = 0,     /* FP32 throughout */
+    ASTRO_FORM_PRECISION = 1  /* FP64 positions and build reductions, FP32
+                                 traversal with compensated sums relative to a
+                                 per-system origin (PHYSICAL preset only) */
+} astro_form;
+
+/* Bit flags for astro_params.flags. */
+#define ASTRO_FLAG_IEEE_EXACT 0x1u  /* traversal uses correctly rounded
+                                       div/sqrt and no contraction (slower;
+                                       reproduces the CPU restatement bit for bit) */
+#define ASTRO_FLAG_NO_GRAPH   0x2u  /* astro_step launches kernels directly
+                                       instead of replaying a CUDA graph */
+#define ASTRO_FLAG_PERSISTENT 0x4u  /* traversal runs as a persistent kernel
+                                       with a work-stealing chunk queue */
+
+typedef struct astro_params {
+    uint32_t preset;          /* astro_preset */
+    uint32_t form;            /* astro_form */
+    uint32_t lbits;           /* bits per axis kept in the key, 1..21; 6 in the
+                                 reference (MortonCode.metal:47-50) => 7 layers */
+    uint32_t flags;           /* ASTRO_FLAG_* */
+    float theta;              /* opening angle (Renderer.swift:864: 0.7) */
+    float g;                  /* gravitational constant (BarnesHut.metal:39: 1e11) */
+    float softening;          /* REFERENCE: added to r^2 (BarnesHut.metal:40: 0.01);
+                                 PHYSICAL: Plummer eps, eps^2 added to r^2 */
+    float leaf_min_dist2;     /* REFERENCE: leaf counted only if r^2 > this
+                                 (BarnesHut.metal:70: 50) */
+    float force_clamp;        /* per-component clamp (BarnesHut.metal:100: 1e5) */
+    float quant_offset;       /* REFERENCE quantiser offset (MortonCode.metal:35-37: 1e6) */
+    float damping;            /* REFERENCE velocity damping (BarnesHut.metal:189: 0.9995) */
+    float type_accel_scale[3];/* REFERENCE per-type multiplier (BarnesHut.metal:181-187: 5,5,1) */
+    uint32_t bucket;          /* PHYSICAL: an opened node holding <= bucket
+                                 particles is summed particle by particle
+                                 (0 = only at layer 0) */
+    uint32_t block_warps;     /* traversal: warps per block (0 = autotuned/default) */
+    uint32_t _reserved[6];
+} astro_params;
+
+/* Fill *out with the defaults of a preset. */
+int astro_params_default(uint32_t preset, astro_params* out);
+
+/* ---------------------------------------------------------------------------
+ * Context: the Renderer's buffers (Renderer.swift:336-391) and its per-frame
+ * compute section (Renderer.swift:495-542).
+ * ------------------------------------------------------------------------- */
+typedef struct astro_ctx astro_ctx;
+
+/* Allocate a context for up to max_n particles in up to max_systems systems.
+ * Replaces Renderer.makeBuffers (Renderer.swift:336-391). */
+int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_systems,
+                 astro_ctx** out);
+int astro_destroy(astro_ctx* ctx);
+int astro_set_params(astro_ctx* ctx, const astro_params* params);
+int astro_get_params(const astro_ctx* ctx, astro_params* out);
+
+/* Upload one system. The first n_tree particles are inserted in the tree
+ * (Renderer.swift:36 octreeCount); all n feel the force. ct may be NULL:
+ * particles below n_tree are then type 1, the rest type 2.
+ * PHYSICAL requires n_tree == n. Replaces Renderer.makeSpheres' buffer copy
+ * (Renderer.swift:490-492). */
+int astro_upload(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                 const ColorType* ct, uint32_t n, uint32_t n_tree);
+
+/* Upload nsys independent systems laid out back to back (PHYSICAL only).
+ * Each system gets its own tree; keys carry the system id in their high bits. */
+int astro_upload_systems(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                         const uint32_t* sys_sizes, uint32_t nsys);
+
+/* Copy the particle state back (waits for the stream). */
+int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n);
+
+/* Stage calls, in step order. Each is stream-ordered and does not wait. */
+int astro_encode(astro_ctx* ctx);    /* generateMortonCodes + fillIndices (MortonCode.metal:26-52, Octree.metal:39-51) */
+int astro_sort(astro_ctx* ctx);      /* radixSorter.sort at layer 0 (Renderer.swift:522-528) */
+int astro_build(astro_ctx* ctx);     /* countUniqueMortonCodes + aggregateLeafNodes + buildInternalNodes (Renderer.swift:529-533,714-755) */
+int astro_traverse(astro_ctx* ctx);  /* barnesHut (BarnesHut.metal:22-101) */
+int astro_integrate(astro_ctx* ctx, float dt); /* updateSpheres (BarnesHut.metal:169-196) */
+
+/* nsteps full steps. REFERENCE: encode, sort, build, traverse, integrate.
+ * PHYSICAL: kick(dt/2)+drift(dt), encode, sort, build, traverse+kick(dt/2),
+ * with one extra force evaluation the first time after an upload. */
+int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps);
+int astro_synchronize(astro_ctx* ctx);
+
+/* Readbacks (wait for the stream). */
+int astro_read_keys(astro_ctx* ctx, uint64_t* codes, uint64_t* sorted_codes,
+                    uint32_t* sorted_indices, uint32_t n);
+/* layer_sizes/offsets: closed-form capacity (Renderer.swift:373-386);
+ * layer_counts: live nodes per layer (the reference's parentCount per layer). */
+int astro_read_tree_info(astro_ctx* ctx, uint32_t* n_layers, uint32_t* layer_sizes,
+                         uint32_t* layer_offsets, uint32_t* layer_counts,
+                         uint32_t max_layers);
+/* AoS nodes [first, first+count) in the reference layout; slots past a
+ * layer's live count read as the cleared node of clearOctreeNodeBuffer
+ * (Octree.metal:253-269). */
+int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t count);
+/* Accelerations (the reference's forceBuffer, float3 with 16-byte stride). */
+int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n);
+/* Traversal statistics of the last traversal: total interactions (monopole +
+ * particle-particle) and nodes visited, summed over particles. */
+int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits);
+
+/* FP64 direct-sum accelerations (G, eps as the context's PHYSICAL params) of
+ * the sampled particles against all particles of their own system, computed
+ * on the device from the current positions. acc3 holds 3 doubles per sample. */
+int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t n_sample,
+                           double* acc3);
+
+/* Device pointer access for callers that own their own kernels. */
+int astro_get_stream(astro_ctx* ctx, void** stream);
+
+const char* astro_last_error(const astro_ctx* ctx);
+const char* astro_version(void);
+const char* astro_status_string(int status);
+
+/* ---------------------------------------------------------------------------
+ * Stand-alone sort: MetalKernelsRadixSort.sort (Astro/RadixSort.swift:98-185).
+ * Stable ascending sort of (uint64 key, uint32 index) pairs. The element
+ * count is read on the device from d_actual_count (NULL => estimated_length);
+ * the launch is sized by estimated_length. d_input_indices NULL => 0..n-1.
+ * Inputs are not modified. Only the low key_bits bits of each key take part
+ * (key_bits = 64 reproduces the reference's 64 one-bit passes exactly;
+ * fewer bits give the same permutation when the high bits are zero).
+ * Temporary device memory is supplied by the caller.
+ * ------------------------------------------------------------------------- */
+int astro_radix_sort_temp_bytes(uint32_t max_length, uint32_t key_bits, size_t* bytes);
+int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
+                     uint64_t* d_output, uint32_t* d_output_indices,
+                     uint32_t estimated_length, const uint32_t* d_actual_count,
+                     uint32_t key_bits, void* d_temp, size_t temp_bytes,
+                     void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Seeded initial conditions (host side, FP64 then cast). Counter-based
+ * Philox4x32-10 streams keyed by (seed, system, particle), so any host
+ * produces identical sets. Replaces Renderer.makeSpheres (Renderer.swift:441-493).
+ * ------------------------------------------------------------------------- */
+typedef enum astro_ic_kind {
+    ASTRO_IC_PLUMMER = 0,      /* scale a = p0, mass M = p1, equilibrium velocities */
+    ASTRO_IC_DISK_BULGE = 1,   /* exponential disk R_d = 1, z_d = 0.1 (80%) + Hernquist bulge (20%), M = 1 */
+    ASTRO_IC_TWO_PLUMMER = 2,  /* two Plummer spheres a = 1, M = 0.5 each, separation p0 on a parabolic approach */
+    ASTRO_IC_UNIFORM_CUBE = 3, /* unit cube, Gaussian velocities sigma = p0, log-normal masses sigma = p1, total 1 */
+    ASTRO_IC_REFERENCE_SCENE = 4 /* the reference's scene: p0 stars, p1 planets, rest dust (Renderer.swift:25-46,441-493) */
+} astro_ic_kind;
+
+int astro_generate_ic(uint32_t kind, uint64_t seed, uint32_t system, uint32_t n,
+                      double p0, double p1, PositionMass* pm, VelocityRadius* vr,
+                      ColorType* ct /* may be NULL */);
+/* nsys sizes drawn log-uniformly in [n_min, n_max] and, when scales is not
+ * NULL, one scale radius per system uniform in [a_min, a_max]. */
+int astro_generate_system_sizes(uint64_t seed, uint32_t nsys, uint32_t n_min, uint32_t n_max,
+                                double a_min, double a_max, uint32_t* sizes, double* scales);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* ASTRO_CUDA_H */

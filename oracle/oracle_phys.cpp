@@ -1,0 +1,547 @@
+// ORACLE — test infrastructure only (see astro_oracle.h). Not part of the product.
+//
+// PHYSICAL preset: the reference's pipeline (Renderer.draw, Renderer.swift:
+// 495-755) with physical units. Stage by stage:
+//   bounding box    per system, FP32 (FP64 in the precision form)
+//   encode          generateMortonCodes (MortonCode.metal:26-52) with a
+//                   bounding-box quantiser into [0, 2^21) and the system id
+//                   above the 3*lbits key bits
+//   sort            MetalKernelsRadixSort.sort (RadixSort.swift:98-185),
+//                   one-bit split passes
+//   run detection   markUniques/scatterUniques per layer (Octree.metal:282-334)
+//   aggregation     aggregateLeafNodes / aggregateNodes (Octree.metal:53-202)
+//                   as raw sums (S = sum m x, M = sum m) in sorted order, the
+//                   last leaf ending at the particle count
+//   traversal       barnesHut (BarnesHut.metal:22-101) with the geometric cell
+//                   size, Plummer softening and particle-particle sums in
+//                   opened leaves and buckets
+//   integration     updateSpheres' kick-drift (BarnesHut.metal:189-194)
+//                   without damping or type multipliers: v += a dt, x += v dt,
+//                   i.e. leapfrog with velocities at half steps
+// State order: the particle arrays are kept in the Morton order of the last
+// step (upload order at first). Each step stable-sorts the keys of the
+// current order and permutes the state by the result, so ties are broken by
+// the previous order. Particle ids map the state back to upload order.
+// Arithmetic: FP32 round-to-nearest without contraction, 1/sqrt as a
+// correctly rounded sqrt followed by a division, sums in ascending order.
+#include "astro_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+constexpr uint64_t kInvalidCode = ASTRO_INVALID_MORTON_CODE;
+constexpr uint32_t kInvalidChild = ASTRO_INVALID_CHILD;
+constexpr float kQuantCells = 2097152.0f;  // 2^21 cells per axis
+constexpr uint32_t kQuantMax = 2097151u;
+
+inline uint32_t float_to_uint_sat(float f) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+inline uint32_t quantise(float x, float lo, float scale) {
+    float t = (x - lo) * scale;
+    return std::min(float_to_uint_sat(t), kQuantMax);
+}
+
+uint32_t system_bits(uint32_t nsys) {
+    uint32_t b = 0;
+    while ((1ull << b) < nsys) ++b;
+    return b;
+}
+
+struct SysQuant {
+    float lo[3];
+    float scale;
+    float ext;
+    float crit2[ASTRO_MAX_LAYERS];
+    double origin[3];
+};
+
+struct PhysState {
+    astro_params p{};
+    uint32_t n = 0, nsys = 1, lbits = 6, layers = 7, sysbits = 0;
+    bool prec = false;
+    std::vector<uint32_t> sys_off, sys_of;
+    std::vector<float> pos, vel, acc, rel;  // float4 per particle, current order
+    std::vector<uint32_t> id;               // upload index of each particle
+    std::vector<double> x64;                // 3 per particle (precision form)
+    std::vector<SysQuant> quant;
+    std::vector<uint64_t> keys, sorted;
+    std::vector<uint32_t> perm;
+    std::vector<uint32_t> sizes, offsets, counts;
+    uint64_t capacity = 0;
+    std::vector<float> cm;       // com.xyz, mass per node
+    std::vector<float> sum32;    // Sx, Sy, Sz, M per node (plain)
+    std::vector<double> sum64;   // Sx, Sy, Sz, M per node (precision)
+    std::vector<uint32_t> pbeg, pend, cbeg, cend;
+    uint64_t interactions = 0, visits = 0;
+
+    void layout(const uint32_t* sys_sizes) {
+        sys_off.assign(nsys + 1, 0);
+        for (uint32_t s = 0; s < nsys; ++s) sys_off[s + 1] = sys_off[s] + sys_sizes[s];
+        sys_of.resize(n);
+        for (uint32_t s = 0; s < nsys; ++s)
+            for (uint32_t i = sys_off[s]; i < sys_off[s + 1]; ++i) sys_of[i] = s;
+        // Closed-form capacity of Renderer.swift:373-386, summed per system.
+        sizes.assign(layers, 0);
+        offsets.assign(layers, 0);
+        uint64_t off = 0;
+        for (uint32_t l = 0; l < layers; ++l) {
+            uint32_t bits = 3u * (lbits - l);
+            uint64_t possible = bits >= 40 ? (1ull << 40) : (1ull << bits);
+            uint64_t size = 0;
+            for (uint32_t s = 0; s < nsys; ++s) size += std::min<uint64_t>(sys_sizes[s], possible);
+            sizes[l] = (uint32_t)size;
+            offsets[l] = (uint32_t)off;
+            off += size;
+        }
+        capacity = off;
+        counts.assign(layers, 0);
+        cm.assign(4 * capacity, 0.0f);
+        sum32.assign(prec ? 0 : 4 * capacity, 0.0f);
+        sum64.assign(prec ? 4 * capacity : 0, 0.0);
+        pbeg.assign(capacity, 0);
+        pend.assign(capacity, 0);
+        cbeg.assign(capacity, 0);
+        cend.assign(capacity, 0);
+    }
+
+    // Bounding box, quantiser and opening thresholds per system.
+    void setup_quant() {
+        quant.assign(nsys, SysQuant{});
+        for (uint32_t s = 0; s < nsys; ++s) {
+            SysQuant& q = quant[s];
+            float lo[3], hi[3];
+            if (prec) {
+                double lo64[3], hi64[3];
+                for (int a = 0; a < 3; ++a) {
+                    lo64[a] = INFINITY;
+                    hi64[a] = -INFINITY;
+                }
+                for (uint32_t i = sys_off[s]; i < sys_off[s + 1]; ++i)
+                    for (int a = 0; a < 3; ++a) {
+                        lo64[a] = std::min(lo64[a], x64[3ull * i + a]);
+                        hi64[a] = std::max(hi64[a], x64[3ull * i + a]);
+                    }
+                for (int a = 0; a < 3; ++a) {
+                    q.origin[a] = (lo64[a] + hi64[a]) * 0.5;
+                    lo[a] = (float)(lo64[a] - q.origin[a]);
+                    hi[a] = (float)(hi64[a] - q.origin[a]);
+                }
+                for (uint32_t i = sys_off[s]; i < sys_off[s + 1]; ++i) {
+                    for (int a = 0; a < 3; ++a)
+                        rel[4ull * i + a] = (float)(x64[3ull * i + a] - q.origin[a]);
+                    rel[4ull * i + 3] = pos[4ull * i + 3];
+                }
+            } else {
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = INFINITY;
+                    hi[a] = -INFINITY;
+                    q.origin[a] = 0.0;
+                }
+                for (uint32_t i = sys_off[s]; i < sys_off[s + 1]; ++i)
+                    for (int a = 0; a < 3; ++a) {
+                        lo[a] = std::min(lo[a], pos[4ull * i + a]);
+                        hi[a] = std::max(hi[a], pos[4ull * i + a]);
+                    }
+                for (uint32_t i = sys_off[s]; i < sys_off[s + 1]; ++i)
+                    for (int a = 0; a < 4; ++a) rel[4ull * i + a] = pos[4ull * i + a];
+            }
+            float ext = 0.0f;
+            for (int a = 0; a < 3; ++a) {
+                q.lo[a] = lo[a];
+                ext = std::max(ext, hi[a] - lo[a]);
+            }
+            if (!(ext > 0.0f) || !std::isfinite(ext)) ext = 1.0f;
+            q.ext = ext;
+            q.scale = kQuantCells / ext;
+            for (uint32_t l = 0; l < layers; ++l) {
+                float size = std::ldexp(ext, (int)l - (int)lbits);
+                float c = size / p.theta;
+                q.crit2[l] = c * c;
+            }
+        }
+    }
+
+    void encode() {
+        const uint32_t unused_bits = 63u - 3u * lbits;
+        keys.resize(n);
+#pragma omp parallel for schedule(static)
+        for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+            uint32_t i = (uint32_t)ii, s = sys_of[i];
+            const SysQuant& q = quant[s];
+            uint32_t qx = quantise(rel[4ull * i + 0], q.lo[0], q.scale);
+            uint32_t qy = quantise(rel[4ull * i + 1], q.lo[1], q.scale);
+            uint32_t qz = quantise(rel[4ull * i + 2], q.lo[2], q.scale);
+            uint64_t code = oracle_interleave_bits(qx, qy, qz) >> unused_bits;
+            keys[i] = ((uint64_t)s << (3u * lbits)) | code;
+        }
+    }
+
+    void sort(uint32_t split_passes) {
+        std::vector<uint32_t> iota(n);
+        for (uint32_t i = 0; i < n; ++i) iota[i] = i;
+        sorted.resize(n);
+        perm.resize(n);
+        uint32_t passes = split_passes ? split_passes : 3u * lbits + sysbits;
+        oracle_split_sort(keys.data(), iota.data(), sorted.data(), perm.data(), n, passes);
+        // Permute the state into the new order.
+        std::vector<float> p2(4ull * n), v2(4ull * n), r2(4ull * n);
+        std::vector<uint32_t> id2(n);
+        std::vector<double> x2(prec ? 3ull * n : 0);
+        for (uint32_t j = 0; j < n; ++j) {
+            uint32_t s = perm[j];
+            for (int a = 0; a < 4; ++a) {
+                p2[4ull * j + a] = pos[4ull * s + a];
+                v2[4ull * j + a] = vel[4ull * s + a];
+                r2[4ull * j + a] = rel[4ull * s + a];
+            }
+            if (prec)
+                for (int a = 0; a < 3; ++a) x2[3ull * j + a] = x64[3ull * s + a];
+            id2[j] = id[s];
+        }
+        pos.swap(p2);
+        vel.swap(v2);
+        rel.swap(r2);
+        id.swap(id2);
+        if (prec) x64.swap(x2);
+    }
+
+    // Run detection per layer (markUniques / scatterUniques, Octree.metal:282-334):
+    // layer 0 runs of equal keys, layer l runs of equal code >> 3 among the
+    // layer l-1 nodes. Children and particle ranges are contiguous.
+    void topology() {
+        std::vector<uint32_t> flags, scan;
+        flags.assign(n, 0);
+        scan.assign(n, 0);
+        for (uint32_t i = 0; i < n; ++i) flags[i] = (i == 0 || sorted[i] != sorted[i - 1]) ? 1u : 0u;
+        oracle_exclusive_scan(flags.data(), scan.data(), n);
+        uint32_t u0 = scan[n - 1] + flags[n - 1];
+        counts[0] = u0;
+        for (uint32_t i = 0; i < n; ++i)
+            if (flags[i]) pbeg[scan[i]] = i;
+        for (uint32_t j = 0; j < u0; ++j) pend[j] = (j + 1 < u0) ? pbeg[j + 1] : n;
+        for (uint32_t l = 1; l < layers; ++l) {
+            uint32_t prev = counts[l - 1], in_off = offsets[l - 1], out_off = offsets[l];
+            flags.assign(prev, 0);
+            scan.assign(prev, 0);
+            for (uint32_t j = 0; j < prev; ++j) {
+                uint64_t c = sorted[pbeg[in_off + j]] >> (3u * l);
+                uint64_t cp = j ? sorted[pbeg[in_off + j - 1]] >> (3u * l) : 0;
+                flags[j] = (j == 0 || c != cp) ? 1u : 0u;
+            }
+            oracle_exclusive_scan(flags.data(), scan.data(), prev);
+            uint32_t u = scan[prev - 1] + flags[prev - 1];
+            counts[l] = u;
+            for (uint32_t j = 0; j < prev; ++j)
+                if (flags[j]) cbeg[out_off + scan[j]] = in_off + j;
+            for (uint32_t k = 0; k < u; ++k) {
+                uint32_t node = out_off + k;
+                cend[node] = (k + 1 < u) ? cbeg[node + 1] : in_off + prev;
+                pbeg[node] = pbeg[cbeg[node]];
+                pend[node] = pend[cend[node] - 1];
+            }
+        }
+    }
+
+    void aggregate() {
+        for (uint32_t l = 0; l < layers; ++l) {
+            uint32_t off = offsets[l], u = counts[l];
+#pragma omp parallel for schedule(dynamic, 64)
+            for (int64_t kk = 0; kk < (int64_t)u; ++kk) {
+                uint32_t node = off + (uint32_t)kk;
+                if (prec) {
+                    double sx = 0, sy = 0, sz = 0, m = 0;
+                    if (l == 0) {
+                        for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
+                            uint32_t s = sys_of[i];
+                            double mi = (double)pos[4ull * i + 3];
+                            m += mi;
+                            sx += mi * (x64[3ull * i + 0] - quant[s].origin[0]);
+                            sy += mi * (x64[3ull * i + 1] - quant[s].origin[1]);
+                            sz += mi * (x64[3ull * i + 2] - quant[s].origin[2]);
+                        }
+                    } else {
+                        for (uint32_t c = cbeg[node]; c < cend[node]; ++c) {
+                            sx += sum64[4ull * c + 0];
+                            sy += sum64[4ull * c + 1];
+                            sz += sum64[4ull * c + 2];
+                            m += sum64[4ull * c + 3];
+                        }
+                    }
+                    double* o = &sum64[4ull * node];
+                    o[0] = sx;
+                    o[1] = sy;
+                    o[2] = sz;
+                    o[3] = m;
+                    float* c = &cm[4ull * node];
+                    c[0] = m > 0 ? (float)(sx / m) : 0.0f;
+                    c[1] = m > 0 ? (float)(sy / m) : 0.0f;
+                    c[2] = m > 0 ? (float)(sz / m) : 0.0f;
+                    c[3] = (float)m;
+                } else {
+                    float sx = 0, sy = 0, sz = 0, m = 0;
+                    if (l == 0) {
+                        for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
+                            const float* q = &pos[4ull * i];
+                            m += q[3];
+                            sx += q[3] * q[0];
+                            sy += q[3] * q[1];
+                            sz += q[3] * q[2];
+                        }
+                    } else {
+                        for (uint32_t c = cbeg[node]; c < cend[node]; ++c) {
+                            sx += sum32[4ull * c + 0];
+                            sy += sum32[4ull * c + 1];
+                            sz += sum32[4ull * c + 2];
+                            m += sum32[4ull * c + 3];
+                        }
+                    }
+                    float* o = &sum32[4ull * node];
+                    o[0] = sx;
+                    o[1] = sy;
+                    o[2] = sz;
+                    o[3] = m;
+                    float* c = &cm[4ull * node];
+                    c[0] = m > 0 ? sx / m : 0.0f;
+                    c[1] = m > 0 ? sy / m : 0.0f;
+                    c[2] = m > 0 ? sz / m : 0.0f;
+                    c[3] = m;
+                }
+            }
+        }
+    }
+
+    // barnesHut (BarnesHut.metal:22-101) per particle in sorted order, then
+    // the fused kick-drift. Children are pushed in order and popped last
+    // first, as the reference's stack does.
+    void traverse_and_integrate(float dt) {
+        const float g = p.g, eps2 = p.softening * p.softening, clampv = p.force_clamp;
+        const uint32_t bucket = p.bucket;
+        const bool kahan = prec;
+        uint64_t tot_inter = 0, tot_visits = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : tot_inter, tot_visits)
+        for (int64_t ipp = 0; ipp < (int64_t)n; ++ipp) {
+            uint32_t ip = (uint32_t)ipp, s = sys_of[ip];
+            const float* crit2 = quant[s].crit2;
+            const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
+            float ax = 0, ay = 0, az = 0, cx = 0, cy = 0, cz = 0;
+            uint64_t inter = 0, vis = 0;
+            auto add = [&](float dx, float dy, float dz, float r2t, float m) {
+                float r2 = r2t + eps2;
+                float inv = 1.0f / std::sqrt(r2);
+                float inv3 = (inv * inv) * inv;
+                float sc = (g * m) * inv3;
+                float tx = dx * sc, ty = dy * sc, tz = dz * sc;
+                if (kahan) {
+                    float y, t;
+                    y = tx - cx; t = ax + y; cx = (t - ax) - y; ax = t;
+                    y = ty - cy; t = ay + y; cy = (t - ay) - y; ay = t;
+                    y = tz - cz; t = az + y; cz = (t - az) - y; az = t;
+                } else {
+                    ax += tx;
+                    ay += ty;
+                    az += tz;
+                }
+                ++inter;
+            };
+            std::vector<uint32_t> st_node, st_layer;
+            st_node.reserve(8 * layers + 8);
+            st_layer.reserve(8 * layers + 8);
+            st_node.push_back(offsets[lbits] + s);
+            st_layer.push_back(lbits);
+            while (!st_node.empty()) {
+                uint32_t nd = st_node.back(), l = st_layer.back();
+                st_node.pop_back();
+                st_layer.pop_back();
+                ++vis;
+                const float* c = &cm[4ull * nd];
+                float dx = c[0] - px, dy = c[1] - py, dz = c[2] - pz;
+                float r2t = dx * dx + dy * dy + dz * dz;
+                if (r2t > crit2[l]) {
+                    add(dx, dy, dz, r2t, c[3]);
+                } else if (l == 0 || pend[nd] - pbeg[nd] <= bucket) {
+                    for (uint32_t j = pbeg[nd]; j < pend[nd]; ++j) {
+                        if (j == ip) continue;
+                        const float* q = &rel[4ull * j];
+                        float ex = q[0] - px, ey = q[1] - py, ez = q[2] - pz;
+                        add(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3]);
+                    }
+                } else {
+                    for (uint32_t ch = cbeg[nd]; ch < cend[nd]; ++ch) {
+                        st_node.push_back(ch);
+                        st_layer.push_back(l - 1);
+                    }
+                }
+            }
+            float* o = &acc[4ull * ip];
+            o[0] = std::fmin(std::fmax(ax, -clampv), clampv);
+            o[1] = std::fmin(std::fmax(ay, -clampv), clampv);
+            o[2] = std::fmin(std::fmax(az, -clampv), clampv);
+            o[3] = 0.0f;
+            tot_inter += inter;
+            tot_visits += vis;
+        }
+        interactions = tot_inter;
+        visits = tot_visits;
+        // Kick-drift (BarnesHut.metal:189-194 without damping and type scale).
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)n; ++i)
+            for (int a = 0; a < 3; ++a) {
+                float v = vel[4ull * i + a] + acc[4ull * i + a] * dt;
+                vel[4ull * i + a] = v;
+                if (prec)
+                    x64[3ull * i + a] = x64[3ull * i + a] + (double)v * (double)dt;
+                else
+                    pos[4ull * i + a] = pos[4ull * i + a] + v * dt;
+            }
+    }
+
+    void step(uint32_t split_passes, float dt) {
+        setup_quant();
+        encode();
+        sort(split_passes);
+        topology();
+        aggregate();
+        traverse_and_integrate(dt);
+    }
+
+    void write_outputs(oracle_outputs* out) {
+        if (!out) return;
+        if (out->codes)
+            for (uint32_t j = 0; j < n; ++j) out->codes[id[j]] = sorted[j];
+        if (out->sorted_codes) std::memcpy(out->sorted_codes, sorted.data(), 8ull * n);
+        if (out->sorted_indices) std::memcpy(out->sorted_indices, id.data(), 4ull * n);
+        if (out->layer_counts) std::memcpy(out->layer_counts, counts.data(), 4ull * layers);
+        if (out->layer_sizes) std::memcpy(out->layer_sizes, sizes.data(), 4ull * layers);
+        if (out->layer_offsets) std::memcpy(out->layer_offsets, offsets.data(), 4ull * layers);
+        if (out->acc4)
+            for (uint32_t j = 0; j < n; ++j)
+                std::memcpy(&out->acc4[4ull * id[j]], &acc[4ull * j], 16);
+        out->interactions = interactions;
+        out->node_visits = visits;
+        if (out->nodes) {
+            for (uint64_t i = 0; i < capacity; ++i) {
+                OctreeNode& o = out->nodes[i];
+                std::memset(&o, 0, sizeof(o));
+                o.mortonCode = kInvalidCode;
+                for (int c = 0; c < 8; ++c) o.children[c] = kInvalidChild;
+            }
+            for (uint32_t l = 0; l < layers; ++l)
+                for (uint32_t k = 0; k < counts[l]; ++k) {
+                    uint32_t node = offsets[l] + k;
+                    OctreeNode& o = out->nodes[node];
+                    o.mortonCode = sorted[pbeg[node]] >> (3u * l);
+                    for (int a = 0; a < 3; ++a) o.centerOfMass[a] = cm[4ull * node + a];
+                    o.totalMass = cm[4ull * node + 3];
+                    o.layer = l;
+                    if (l > 0)
+                        for (uint32_t c = cbeg[node], q = 0; c < cend[node] && q < 8; ++c, ++q)
+                            o.children[q] = c;
+                }
+        }
+    }
+};
+
+}  // namespace
+
+extern "C" int oracle_phys_run(const astro_params* p, PositionMass* pm, VelocityRadius* vr,
+                               uint32_t n, const uint32_t* sys_sizes, uint32_t nsys, float dt,
+                               uint32_t nsteps, uint32_t split_passes, double* pos64,
+                               oracle_outputs* out) {
+    if (!p || !pm || !vr || n == 0 || p->lbits < 1 || p->lbits > 21) return -1;
+    uint32_t one = n;
+    if (!sys_sizes) {
+        sys_sizes = &one;
+        nsys = 1;
+    }
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < nsys; ++s) {
+        if (sys_sizes[s] == 0) return -1;
+        total += sys_sizes[s];
+    }
+    if (total != n) return -1;
+    PhysState st;
+    st.p = *p;
+    st.n = n;
+    st.nsys = nsys;
+    st.lbits = p->lbits;
+    st.layers = p->lbits + 1;
+    st.sysbits = nsys > 1 ? system_bits(nsys) : 0;
+    if (3u * st.lbits + st.sysbits > 64) return -1;
+    st.prec = p->form == ASTRO_FORM_PRECISION;
+    st.pos.resize(4ull * n);
+    st.vel.resize(4ull * n);
+    st.acc.assign(4ull * n, 0.0f);
+    st.rel.resize(4ull * n);
+    st.id.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int a = 0; a < 3; ++a) {
+            st.pos[4ull * i + a] = pm[i].position[a];
+            st.vel[4ull * i + a] = vr[i].velocity[a];
+        }
+        st.pos[4ull * i + 3] = pm[i].mass;
+        st.vel[4ull * i + 3] = vr[i].radius;
+        st.id[i] = i;
+    }
+    if (st.prec) {
+        st.x64.resize(3ull * n);
+        for (uint32_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) st.x64[3ull * i + a] = (double)pm[i].position[a];
+    }
+    st.layout(sys_sizes);
+    for (uint32_t s = 0; s < nsteps; ++s) st.step(split_passes, dt);
+    st.write_outputs(out);
+    for (uint32_t j = 0; j < n; ++j) {
+        uint32_t i = st.id[j];
+        for (int a = 0; a < 3; ++a) {
+            pm[i].position[a] = st.prec ? (float)st.x64[3ull * j + a] : st.pos[4ull * j + a];
+            vr[i].velocity[a] = st.vel[4ull * j + a];
+        }
+        if (pos64 && st.prec)
+            for (int a = 0; a < 3; ++a) pos64[3ull * i + a] = st.x64[3ull * j + a];
+    }
+    return 0;
+}
+
+extern "C" void oracle_direct_accel_f64(const PositionMass* pm, const double* pos64, uint32_t n,
+                                        const uint32_t* sys_sizes, uint32_t nsys,
+                                        const uint32_t* sample_idx, uint32_t n_sample, double g,
+                                        double eps, double* acc3) {
+    std::vector<uint32_t> off(1, 0);
+    if (!sys_sizes) {
+        off.push_back(n);
+    } else {
+        for (uint32_t s = 0; s < nsys; ++s) off.push_back(off.back() + sys_sizes[s]);
+    }
+    auto X = [&](uint32_t i, int a) {
+        return pos64 ? pos64[3ull * i + a] : (double)pm[i].position[a];
+    };
+    const double eps2 = eps * eps;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t k = 0; k < (int64_t)n_sample; ++k) {
+        uint32_t i = sample_idx[k];
+        uint32_t s = (uint32_t)(std::upper_bound(off.begin(), off.end(), i) - off.begin()) - 1;
+        double xi = X(i, 0), yi = X(i, 1), zi = X(i, 2);
+        double ax = 0, ay = 0, az = 0;
+        for (uint32_t j = off[s]; j < off[s + 1]; ++j) {
+            if (j == i) continue;
+            double dx = X(j, 0) - xi, dy = X(j, 1) - yi, dz = X(j, 2) - zi;
+            double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            double inv = 1.0 / std::sqrt(r2);
+            double w = g * (double)pm[j].mass * inv * inv * inv;
+            ax += w * dx;
+            ay += w * dy;
+            az += w * dz;
+        }
+        acc3[3 * k] = ax;
+        acc3[3 * k + 1] = ay;
+        acc3[3 * k + 2] = az;
+    }
+}

@@ -1,0 +1,367 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU restatement.
+
+Bit-exact: Morton keys, sort permutation, layer sizes/offsets/live counts,
+node records (codes, children, layers, masses, centres of mass) and, in the
+REFERENCE preset and the IEEE-exact PHYSICAL traversal, accelerations and the
+integrated state.
+Tolerance: the fast PHYSICAL traversal (rsqrt and FMA) differs from the
+restatement only by rounding in each interaction; its accelerations must
+satisfy |a_gpu - a_cpu| <= 2e-5 |a_cpu| + 1e-6 median|a_cpu| per particle,
+and the opening decisions (interaction and visit counts) must be identical.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+ACC_RTOL = 2e-5
+ACC_ATOL_REL = 1e-6
+
+
+def load(name):
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+@pytest.fixture(scope="module")
+def ag(native):
+    return native
+
+
+def particles(L, pos, masses=None):
+    pm, vr = L.empty_particles(len(pos))
+    pm["position"] = np.asarray(pos, np.float32)
+    pm["mass"] = 1.0 if masses is None else np.asarray(masses, np.float32)
+    return pm, vr
+
+
+def run_gpu(ag, params, pm, vr, ct=None, n_tree=None, dt=0.0, steps=1, sizes=None):
+    with ag.Simulation(params, max_n=len(pm), max_systems=max(1, len(sizes or [1]))) as sim:
+        if sizes is not None:
+            sim.upload_systems(pm, vr, sizes)
+        else:
+            sim.upload(pm, vr, ct, n_tree=n_tree)
+        sim.draw(dt, steps)
+        codes, sorted_codes, idx = sim.read_keys()
+        sizes_, offsets, counts = sim.tree_info()
+        out = dict(codes=codes, sorted_codes=sorted_codes, sorted_indices=idx,
+                   layer_sizes=sizes_, layer_offsets=offsets, layer_counts=counts,
+                   nodes=sim.read_nodes(), acc4=sim.read_accel())
+        out["interactions"], out["node_visits"] = sim.read_stats()
+        out["pm"], out["vr"] = sim.download()
+    return out
+
+
+def assert_tree_equal(gpu, ref):
+    for k in ["codes", "sorted_codes", "sorted_indices", "layer_sizes", "layer_offsets",
+              "layer_counts"]:
+        assert np.array_equal(gpu[k], ref[k]), k
+    assert gpu["nodes"].shape == ref["nodes"].shape
+    for f in ["mortonCode", "children", "layer", "totalMass", "centerOfMass"]:
+        assert np.array_equal(gpu["nodes"][f], ref["nodes"][f]), f
+    assert np.array_equal(gpu["nodes"], ref["nodes"])
+
+
+def acc_close(gpu, ref):
+    a = ref[:, :3].astype(np.float64)
+    d = np.linalg.norm(gpu[:, :3].astype(np.float64) - a, axis=1)
+    na = np.linalg.norm(a, axis=1)
+    tol = ACC_RTOL * na + ACC_ATOL_REL * np.median(na)
+    return d <= tol, d / np.maximum(na, 1e-30)
+
+
+# ------------------------------------------------------------ REFERENCE --
+
+def test_reference_golden_morton_and_octants(ag, oracle):
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_REFERENCE)
+    g = load("morton")
+    pm, vr = particles(L, [c["pos"] for c in g["cases"]])
+    out = run_gpu(ag, p, pm, vr)
+    assert [int(c) for c in out["codes"]] == [c["key"] for c in g["cases"]]
+    g = load("octants")
+    pm, vr = particles(L, g["positions"])
+    out = run_gpu(ag, p, pm, vr)
+    assert [int(k) for k in out["codes"]] == g["keys"]
+    assert [int(i) for i in out["sorted_indices"]] == g["sorted_indices"]
+    assert list(out["layer_counts"]) == g["layer_counts"]
+    root = out["nodes"][g["root"]]
+    assert list(root["children"]) == g["root_children"] and root["totalMass"] == 8.0
+    ref = oracle.ref_run(p, pm.copy(), vr.copy(), dt=0.0, steps=1)
+    assert_tree_equal(out, ref)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_reference_golden_two_body(ag, oracle, case):
+    L = ag.layouts
+    c = load("two_body")["cases"][case]
+    pm, vr = particles(L, [(c["x0"], 0, 0), (c["x0"] + c["d"], 0, 0)], [c["m"], c["m"]])
+    out = run_gpu(ag, ag.default_params(L.PRESET_REFERENCE), pm, vr)
+    assert out["acc4"][0, 0] == pytest.approx(c["fx0"], rel=1e-5)
+    assert out["acc4"][1, 0] == pytest.approx(c["fx1"], rel=1e-5)
+
+
+def test_reference_golden_last_leaf(ag):
+    L = ag.layouts
+    g = load("last_leaf")
+    pm, vr = particles(L, g["positions"], g["masses"])
+    out = run_gpu(ag, ag.default_params(L.PRESET_REFERENCE), pm, vr)
+    assert list(out["nodes"][:2]["totalMass"]) == g["reference_leaf_mass"]
+    out = run_gpu(ag, ag.default_params(L.PRESET_PHYSICAL), pm, vr)
+    assert list(out["nodes"][:2]["totalMass"]) == g["fixed_leaf_mass"]
+
+
+def test_reference_scene_bit_exact(ag, oracle):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_REFERENCE)
+    pm, vr, ct = ic.reference_scene(5, 200, 5000, seed=21)
+    out = run_gpu(ag, p, pm, vr, ct, n_tree=205, dt=1.0 / 60, steps=3)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.ref_run(p, pm_o, vr_o, ct, n_tree=205, dt=1.0 / 60, steps=3, split_passes=64)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+def test_reference_plummer_all_in_tree(ag, oracle):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_REFERENCE)
+    pm, vr = ic.plummer(16384, seed=1001)
+    pm["position"] *= 4e4  # into the reference's units (positions ~1e6)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.ref_run(p, pm_o, vr_o, dt=1e-3, steps=2, split_passes=18)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o)
+
+
+# ------------------------------------------------------------- PHYSICAL --
+
+@pytest.mark.parametrize("lbits", [6, 10, 21])
+def test_physical_exact_bit_exact(ag, oracle, lbits):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=lbits, flags=L.FLAG_IEEE_EXACT)
+    pm, vr = ic.plummer(16384, seed=1001)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=3)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=1e-3, steps=3)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+@pytest.mark.parametrize("warps,persistent", [(4, False), (2, True), (8, False)])
+def test_physical_fast_within_tolerance(ag, oracle, warps, persistent):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    flags = L.FLAG_PERSISTENT if persistent else 0
+    p = ag.default_params(L.PRESET_PHYSICAL, flags=flags, block_warps=warps, softening=0.005)
+    pm, vr = ic.disk_bulge(32768, seed=1002)
+    out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=1)
+    ref = oracle.phys_run(p, pm.copy(), vr.copy(), dt=5e-4, steps=1)
+    assert_tree_equal(out, ref)
+    ok, rel = acc_close(out["acc4"], ref["acc4"])
+    assert ok.all(), f"{(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
+    assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
+
+
+def test_physical_precision_form_bit_exact(ag, oracle):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, form=L.FORM_PRECISION, flags=L.FLAG_IEEE_EXACT,
+                          softening=0.002, lbits=10)
+    pm, vr = ic.two_plummer(16384, seed=1003)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=3)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=1e-3, steps=3)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_physical_batched_bit_exact(ag, oracle, persistent):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    sizes = [1, 2, 31, 33, 1024, 5000, 64, 3, 4096, 777]
+    parts = [ic.plummer(s, seed=1004, a=0.5 + 0.1 * k, system=k) for k, s in enumerate(sizes)]
+    pm = np.concatenate([a for a, _ in parts])
+    vr = np.concatenate([b for _, b in parts])
+    flags = L.FLAG_IEEE_EXACT | (L.FLAG_PERSISTENT if persistent else 0)
+    p = ag.default_params(L.PRESET_PHYSICAL, flags=flags)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2, sizes=sizes)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, sizes=sizes, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o)
+
+
+def test_graph_replay_equals_eager(ag):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr = ic.plummer(20000, seed=5)
+    res = []
+    for flags in [0, L.FLAG_NO_GRAPH]:
+        p = ag.default_params(L.PRESET_PHYSICAL, flags=flags)
+        with ag.Simulation(p, max_n=len(pm)) as sim:
+            sim.upload(pm, vr)
+            sim.draw(1e-3, 5)
+            res.append(sim.download())
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+
+
+def test_stage_calls_equal_step(ag):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr = ic.plummer(10000, seed=6)
+    p = ag.default_params(L.PRESET_PHYSICAL)
+    with ag.Simulation(p, max_n=len(pm)) as sim:
+        sim.upload(pm, vr)
+        sim.draw(1e-3, 1)
+        a = sim.download()
+    with ag.Simulation(p, max_n=len(pm)) as sim:
+        sim.upload(pm, vr)
+        sim.generate_morton_codes()
+        sim.sort()
+        sim.build_tree()
+        sim.barnes_hut()
+        sim.update_spheres(1e-3)
+        b = sim.download()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_upload_download_round_trip_and_errors(ag):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr = ic.uniform_cube(1000, seed=1)
+    p = ag.default_params(L.PRESET_PHYSICAL)
+    with ag.Simulation(p, max_n=1000) as sim:
+        with pytest.raises(ag.AstroError) as e:
+            sim.barnes_hut()
+        assert e.value.status == -5
+        sim.upload(pm, vr)
+        got_pm, got_vr = sim.download()
+        assert np.array_equal(got_pm["position"], pm["position"])
+        assert np.array_equal(got_pm["mass"], pm["mass"])
+        assert np.array_equal(got_vr["velocity"], vr["velocity"])
+        with pytest.raises(ag.AstroError) as e:
+            sim.barnes_hut()
+        assert e.value.status == -5
+        big_pm, big_vr = ic.uniform_cube(1001, seed=1)
+        with pytest.raises(ag.AstroError) as e:
+            sim.upload(big_pm, big_vr)
+        assert e.value.status == -2
+
+
+def test_direct_sum_f64_matches_cpu(ag, oracle):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr = ic.plummer(30000, seed=8)
+    p = ag.default_params(L.PRESET_PHYSICAL, softening=0.01)
+    samples = np.arange(0, 30000, 97, dtype=np.uint32)
+    with ag.Simulation(p, max_n=len(pm)) as sim:
+        sim.upload(pm, vr)
+        gpu = sim.direct_accel_f64(samples)
+    cpu = oracle.direct_accel(pm, samples, g=1.0, eps=0.01)
+    assert np.allclose(gpu, cpu, rtol=1e-10, atol=1e-12)
+
+
+# ----------------------------------------------------------------- sort --
+
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 100003, 1 << 20, 3_000_017])
+@pytest.mark.parametrize("key_bits", [18, 26, 63, 64])
+def test_radix_sort_matches_stable_argsort(ag, n, key_bits):
+    import torch
+
+    from astro_gb300.radix_sort import RadixSort
+
+    rng = np.random.default_rng(n + key_bits)
+    hi = (1 << key_bits) if key_bits < 64 else None
+    if hi is None:
+        keys = rng.integers(0, 1 << 63, n, dtype=np.uint64) * 2 + rng.integers(0, 2, n).astype(np.uint64)
+    else:
+        keys = rng.integers(0, hi, n, dtype=np.uint64)
+    keys[rng.integers(0, n, n // 3 + 1)] = keys[0]  # duplicates
+    idx_in = rng.permutation(n).astype(np.uint32)
+    dk = torch.from_numpy(keys.view(np.int64)).cuda()
+    di = torch.from_numpy(idx_in.view(np.int32)).cuda()
+    ok = torch.empty_like(dk)
+    oi = torch.empty_like(di)
+    s = RadixSort(n, key_bits)
+    s.sort(dk, di, ok, oi, n)
+    torch.cuda.synchronize()
+    want = np.argsort(keys, kind="stable")
+    assert np.array_equal(ok.cpu().numpy().view(np.uint64), keys[want])
+    assert np.array_equal(oi.cpu().numpy().view(np.uint32), idx_in[want])
+    # Inputs untouched.
+    assert np.array_equal(dk.cpu().numpy().view(np.uint64), keys)
+
+
+def test_radix_sort_device_count_and_iota(ag):
+    import torch
+
+    from astro_gb300.radix_sort import RadixSort
+
+    rng = np.random.default_rng(1)
+    est, count = 50000, 31234
+    keys = rng.integers(0, 1 << 18, est, dtype=np.uint64)
+    dk = torch.from_numpy(keys.view(np.int64)).cuda()
+    ok = torch.full_like(dk, -1)
+    oi = torch.full((est,), -1, dtype=torch.int32, device="cuda")
+    cnt = torch.tensor([count], dtype=torch.int32, device="cuda")
+    s = RadixSort(est, 18)
+    s.sort(dk, None, ok, oi, est, cnt)
+    torch.cuda.synchronize()
+    want = np.argsort(keys[:count], kind="stable")
+    assert np.array_equal(ok.cpu().numpy().view(np.uint64)[:count], keys[:count][want])
+    assert np.array_equal(oi.cpu().numpy().view(np.uint32)[:count], want.astype(np.uint32))
+    # Slots past the count are not written.
+    assert (ok.cpu().numpy()[count:] == -1).all()
+
+
+# ------------------------------------------------ full-size properties --
+
+def test_large_uniform_cube_properties(ag):
+    """16.7M bodies at lbits = 21 (63-bit keys): properties that do not need
+    the CPU restatement."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    n = 1 << 24
+    pm, vr = ic.uniform_cube(n, seed=1005)
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=21, softening=0.001)
+    with ag.Simulation(p, max_n=n) as sim:
+        sim.upload(pm, vr)
+        sim.draw(0.0, 1)
+        codes, sorted_codes, idx = sim.read_keys()
+        sizes, offsets, counts = sim.tree_info()
+        acc = sim.read_accel()
+        samples = np.arange(0, n, n // 2048, dtype=np.uint32)
+        direct = sim.direct_accel_f64(samples)
+        top = sim.read_nodes(int(offsets[-1]), 1)
+    assert np.all(sorted_codes[1:] >= sorted_codes[:-1])
+    assert np.array_equal(np.sort(idx), np.arange(n, dtype=np.uint32))
+    assert np.array_equal(codes[idx], sorted_codes)
+    assert counts[-1] == 1 and np.all(counts[1:] <= counts[:-1])
+    assert top["totalMass"][0] == pytest.approx(1.0, rel=1e-4)
+    err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert np.median(err) < 1e-2

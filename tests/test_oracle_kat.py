@@ -1,0 +1,205 @@
+"""Known-answer tests of the CPU restatement (oracle/) against the hand-derived
+golden vectors in tests/golden (the reference ships none of its own)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from astro_gb300 import layouts as L
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+def ref_params(**kw):
+    """REFERENCE defaults without loading the CUDA library."""
+    p = L.Params(preset=L.PRESET_REFERENCE, form=0, lbits=6, flags=0, theta=0.7, g=1e11,
+                 softening=0.01, leaf_min_dist2=50.0, force_clamp=1e5, quant_offset=1e6,
+                 damping=0.9995, bucket=0, block_warps=0)
+    p.type_accel_scale[0], p.type_accel_scale[1], p.type_accel_scale[2] = 5.0, 5.0, 1.0
+    return p.replace(**kw) if kw else p
+
+
+def phys_params(**kw):
+    p = L.Params(preset=L.PRESET_PHYSICAL, form=0, lbits=6, flags=0, theta=0.7, g=1.0,
+                 softening=0.01, leaf_min_dist2=0.0, force_clamp=1e5, quant_offset=0.0,
+                 damping=1.0, bucket=16, block_warps=0)
+    for i in range(3):
+        p.type_accel_scale[i] = 1.0
+    return p.replace(**kw) if kw else p
+
+
+def particles(pos, masses=None):
+    n = len(pos)
+    pm, vr = L.empty_particles(n)
+    pm["position"] = np.asarray(pos, np.float32)
+    pm["mass"] = 1.0 if masses is None else np.asarray(masses, np.float32)
+    return pm, vr
+
+
+def test_interleave_bit_placement(oracle):
+    for i in range(21):
+        assert oracle.interleave(1 << i, 0, 0) == 1 << (3 * i)
+        assert oracle.interleave(0, 1 << i, 0) == 1 << (3 * i + 1)
+        assert oracle.interleave(0, 0, 1 << i) == 1 << (3 * i + 2)
+    # Bits above 21 are masked off (MortonCode.metal:9-11).
+    assert oracle.interleave(1 << 21, 0, 0) == 0
+
+
+def test_morton_golden(oracle):
+    g = load("morton")
+    pos = [c["pos"] for c in g["cases"]]
+    pm, _ = particles(pos)
+    codes = oracle.morton_codes(pm, g["lbits"], g["offset"])
+    assert [int(c) for c in codes] == [c["key"] for c in g["cases"]]
+
+
+def test_exclusive_scan_beyond_reference_limit(oracle):
+    # The reference's two-level scan stops at 1,048,576 values; the
+    # restatement lifts the limit without changing smaller results.
+    rng = np.random.default_rng(3)
+    for n in [1, 2, 1023, 1024, 1025, 1 << 20, (1 << 20) + 7, 3_000_001]:
+        v = rng.integers(0, 3, n).astype(np.uint32)
+        want = np.concatenate([[0], np.cumsum(v, dtype=np.uint64)[:-1]]).astype(np.uint32)
+        assert np.array_equal(oracle.exclusive_scan(v), want), n
+
+
+def test_split_sort_golden_and_stability(oracle):
+    g = load("sort")
+    keys, perm = oracle.split_sort(np.array(g["keys"], np.uint64), passes=64)
+    assert [int(i) for i in perm] == g["perm"]
+    rng = np.random.default_rng(5)
+    k = rng.integers(0, 1 << 18, 50000).astype(np.uint64)
+    k[::7] = k[3]  # many duplicates
+    ok, oi = oracle.split_sort(k, passes=64)
+    want = np.argsort(k, kind="stable")
+    assert np.array_equal(oi, want) and np.array_equal(ok, k[want])
+    # Skipping the constant-zero high bits gives the identical permutation.
+    ok18, oi18 = oracle.split_sort(k, passes=18)
+    assert np.array_equal(oi18, oi)
+
+
+def test_layer_layout_closed_form(oracle):
+    sizes, offsets, cap = oracle.layer_layout(205, 6)
+    # Renderer.swift:373-386 with octreeCount = 205.
+    assert list(sizes) == [205, 205, 205, 205, 64, 8, 1]
+    assert list(offsets) == [0, 205, 410, 615, 820, 884, 892]
+    assert cap == 893
+    sizes, offsets, cap = oracle.layer_layout(1 << 24, 21)
+    assert sizes[0] == 1 << 24 and sizes[-1] == 1 and sizes[13] == 1 << 24 and sizes[14] == 1 << 21
+
+
+def test_octant_tree_golden(oracle):
+    g = load("octants")
+    pm, vr = particles(g["positions"])
+    out = oracle.ref_run(ref_params(), pm, vr, dt=0.0, steps=1)
+    assert [int(k) for k in out["codes"]] == g["keys"]
+    assert [int(i) for i in out["sorted_indices"]] == g["sorted_indices"]
+    assert list(out["layer_counts"]) == g["layer_counts"]
+    assert list(out["layer_sizes"]) == g["layer_sizes"]
+    assert list(out["layer_offsets"]) == g["layer_offsets"]
+    root = out["nodes"][g["root"]]
+    assert list(root["children"]) == g["root_children"]
+    assert root["totalMass"] == g["root_mass"]
+    assert np.allclose(root["centerOfMass"], g["root_com"], rtol=0, atol=0.5)
+    assert root["layer"] == 6
+    # Every layer-1..5 node has exactly one child.
+    for node in out["nodes"][8:48]:
+        assert node["children"][0] != L.INVALID_CHILD and node["children"][1] == L.INVALID_CHILD
+    for leaf in out["nodes"][:8]:
+        assert all(c == L.INVALID_CHILD for c in leaf["children"])
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_two_body_golden(oracle, case):
+    g = load("two_body")
+    c = g["cases"][case]
+    pm, vr = particles([(c["x0"], 0, 0), (c["x0"] + c["d"], 0, 0)], [c["m"], c["m"]])
+    out = oracle.ref_run(ref_params(), pm, vr, dt=0.0, steps=1)
+    acc = out["acc4"]
+    assert acc[0, 0] == pytest.approx(c["fx0"], rel=1e-5, abs=0)
+    assert acc[1, 0] == pytest.approx(c["fx1"], rel=1e-5, abs=0)
+    assert acc[0, 1] == 0 and acc[0, 2] == 0
+
+
+def test_last_leaf_quirk_reference_and_fix(oracle):
+    g = load("last_leaf")
+    pm, vr = particles(g["positions"], g["masses"])
+    out = oracle.ref_run(ref_params(), pm.copy(), vr.copy(), dt=0.0, steps=1)
+    assert list(out["layer_counts"][:1]) == [2]
+    leaves = out["nodes"][:2]
+    assert list(leaves["totalMass"]) == g["reference_leaf_mass"]
+    assert np.array_equal(leaves["centerOfMass"], np.array(g["reference_leaf_com"], np.float32))
+    out = oracle.phys_run(phys_params(), pm.copy(), vr.copy(), dt=0.0, steps=1)
+    leaves = out["nodes"][:2]
+    assert list(leaves["totalMass"]) == g["fixed_leaf_mass"]
+
+
+def test_reference_integrator(oracle):
+    # updateSpheres (BarnesHut.metal:169-196): a = F * {5,5,1}[type];
+    # v = 0.9995 v + a dt; x += v dt. A lone body feels no force.
+    pm, vr = particles([(10.0, 20.0, 30.0)])
+    vr["velocity"] = [[1.0, 2.0, 3.0]]
+    oracle.ref_run(ref_params(), pm, vr, dt=0.5, steps=1)
+    v = np.float32(0.9995) * np.array([1.0, 2.0, 3.0], np.float32)
+    assert np.array_equal(vr["velocity"][0], v)
+    assert np.array_equal(pm["position"][0], np.array([10, 20, 30], np.float32) + v * np.float32(0.5))
+
+
+def test_physical_tiny_theta_is_direct_sum(oracle, native):
+    # With theta -> 0 nothing is accepted: every opened leaf is summed
+    # particle by particle, which is the softened direct sum.
+    from astro_gb300 import ic  # host generator, no GPU involved
+
+    pm, vr = ic.plummer(2048, seed=11)
+    p = phys_params(theta=1e-6, softening=0.05)
+    out = oracle.phys_run(p, pm.copy(), vr.copy(), dt=0.0, steps=1)
+    samples = np.arange(0, 2048, 7)
+    direct = oracle.direct_accel(pm, samples, g=1.0, eps=0.05)
+    got = out["acc4"][samples, :3].astype(np.float64)
+    err = np.linalg.norm(got - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert np.max(err) < 1e-4
+    assert out["interactions"] == 2048 * 2047
+
+
+def test_physical_error_against_direct_sum(oracle, native):
+    from astro_gb300 import ic
+
+    pm, vr = ic.plummer(8192, seed=1001)
+    out = oracle.phys_run(phys_params(theta=0.5), pm.copy(), vr.copy(), dt=0.0, steps=1)
+    samples = np.arange(0, 8192, 13)
+    direct = oracle.direct_accel(pm, samples, g=1.0, eps=0.01)
+    got = out["acc4"][samples, :3].astype(np.float64)
+    err = np.linalg.norm(got - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert np.median(err) < 5e-3 and np.percentile(err, 99) < 5e-2
+
+
+def test_physical_batched_equals_separate(oracle, native):
+    from astro_gb300 import ic
+
+    pm1, vr1 = ic.plummer(700, seed=3, system=0)
+    pm2, vr2 = ic.plummer(1300, seed=3, a=2.0, system=1)
+    pm = np.concatenate([pm1, pm2])
+    vr = np.concatenate([vr1, vr2])
+    p = phys_params()
+    both = oracle.phys_run(p, pm.copy(), vr.copy(), sizes=[700, 1300], dt=1e-3, steps=2)
+    a = oracle.phys_run(p, pm1.copy(), vr1.copy(), dt=1e-3, steps=2)
+    b = oracle.phys_run(p, pm2.copy(), vr2.copy(), dt=1e-3, steps=2)
+    assert np.array_equal(both["acc4"][:700], a["acc4"])
+    assert np.array_equal(both["acc4"][700:], b["acc4"])
+
+
+def test_precision_form_runs_and_tracks_plain(oracle, native):
+    from astro_gb300 import ic
+
+    pm, vr = ic.plummer(4096, seed=9)
+    plain = oracle.phys_run(phys_params(), pm.copy(), vr.copy(), dt=1e-3, steps=3)
+    prec = oracle.phys_run(phys_params(form=L.FORM_PRECISION), pm.copy(), vr.copy(), dt=1e-3,
+                           steps=3, want_pos64=True)
+    d = np.abs(plain["acc4"] - prec["acc4"]).max() / np.abs(plain["acc4"]).max()
+    assert d < 1e-3
+    assert prec["pos64"].shape == (4096, 3)
