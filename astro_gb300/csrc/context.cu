@@ -437,6 +437,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
         if (e_ != cudaSuccess) return cleanup(cuda_fail(nullptr, e_, #call)); \
     } while (0)
     CKC(cudaGetDevice(&ctx->device));
+    CKC(astro::sort_init());
     CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     for (int b = 0; b < 2; ++b) {
         CKC(dev_alloc(&ctx->pos[b], max_n));
@@ -697,23 +698,17 @@ int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps) {
     NEED_UPLOAD();
     if (!std::isfinite(dt)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "dt must be finite");
     if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "step called between sort and traverse");
-    const bool use_graph = (ctx->p.flags & ASTRO_FLAG_NO_GRAPH) == 0;
-    uint32_t done = 0;
     int r;
-    if (use_graph && nsteps > 1 && !(ctx->graph_valid && ctx->graph_dt == dt)) {
-        // One eager step first (it also completes one-time set-up), then capture.
-        if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
-        done = 1;
-        if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
-    }
-    for (; done < nsteps; ++done) {
-        if (use_graph && ctx->graph_valid && ctx->graph_dt == dt) {
-            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-            ctx->tree_valid = true;
-        } else {
+    if ((ctx->p.flags & ASTRO_FLAG_NO_GRAPH) != 0) {
+        for (uint32_t s = 0; s < nsteps; ++s)
             if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
-        }
+        return ASTRO_OK;
     }
+    // The step is captured once per (upload, params, dt) and replayed.
+    if (nsteps > 0 && !(ctx->graph_valid && ctx->graph_dt == dt))
+        if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
+    for (uint32_t s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    if (nsteps > 0) ctx->tree_valid = true;
     return ASTRO_OK;
 }
 

@@ -45,6 +45,7 @@ struct SortPlan {
     uint32_t passes, ntiles, tile;
 };
 SortPlan sort_plan(uint32_t max_len, uint32_t key_bits);
+cudaError_t sort_init();
 // Stable sort of n_est (key, value) pairs (count read from d_count when not
 // NULL). vals_in NULL => values are 0..n-1. err (device word) collects
 // look-back timeouts; NULL => the word inside temp.

@@ -234,6 +234,17 @@ int num_sms() {
 
 }  // namespace
 
+// One-time kernel attribute (the pass kernel's shared memory exceeds the
+// 48 KB default). Safe to call repeatedly; called before any stream capture.
+cudaError_t sort_init() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(PassSmem));
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
     SortPlan p{};
     p.passes = key_bits == 0 ? 1u : (key_bits + 7u) / 8u;
@@ -265,14 +276,9 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
     if (n_est == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(n_est, key_bits);
     if (temp_bytes < plan.total || key_bits > 64) return cudaErrorInvalidValue;
-    static bool attr_set = false;
     const size_t smem = sizeof(PassSmem);
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    cudaError_t e0 = sort_init();
+    if (e0 != cudaSuccess) return e0;
     char* base = static_cast<char*>(temp);
     uint64_t* keys_tmp = reinterpret_cast<uint64_t*>(base + plan.keys_tmp);
     uint32_t* vals_tmp = reinterpret_cast<uint32_t*>(base + plan.vals_tmp);

@@ -1,0 +1,432 @@
+"""Benchmark of the Barnes-Hut step on GB300: particle-updates/s.
+
+Default workload (the configuration the metric is quoted on): a seeded
+rotating exponential disk (R_d = 1, z_d = 0.1, 80% of the mass) plus a
+Hernquist bulge (20%), N = 524,288, PHYSICAL preset, plain FP32, theta = 0.7,
+eps = 0.005, dt = 5e-4. One step = bbox, encode, sort, Morton reorder, tree
+topology, per-layer aggregation, traversal with the fused kick-drift.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c1|c2|c3|c4|c5] [--form plain|precision]
+
+`value` is the device-timed throughput with inputs resident in HBM (CUDA
+events on the context's stream around each step, L2 flushed before every
+timed step). `e2e` is the same metric through the C ABI with host buffers:
+each step uploads PositionMass/VelocityRadius from pinned host memory, steps
+and downloads them. `--impl reference` times the CPU restatement of the
+reference kernels (oracle/, OpenMP over all host cores) on the same workload.
+Under torchrun every rank runs an independent replica (the single-system step
+does not shard); rank 0 prints the line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-updates/s per GB300 step (plain FP32 vs precision+batched) at stated FP64 error"
+UNIT = "particle-updates/s"
+FLOPS_PER_INTERACTION = 20  # the GPU Gems 3 ch. 31 convention for one softened interaction
+L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+
+WORKLOADS = {
+    # name: (description, generator, n, params overrides, dt)
+    "c1": ("Plummer sphere a=1 N=16384", "plummer", 16384, dict(softening=0.01), 1e-3),
+    "c2": ("exponential disk + Hernquist bulge N=524288", "disk_bulge", 524288,
+           dict(softening=0.005), 5e-4),
+    "c3": ("two Plummer spheres a=1 M=0.5 at separation 10, N=4194304", "two_plummer", 4194304,
+           dict(softening=0.002), 1e-3),
+    "c4": ("256 Plummer systems, N_s log-uniform [1024, 65536]", "batch", 0,
+           dict(softening=0.01), 1e-3),
+    "c5": ("uniform unit cube, log-normal masses, N=16777216", "uniform_cube", 16777216,
+           dict(softening=0.001), 1e-3),
+}
+SEEDS = {"c1": 1001, "c2": 1002, "c3": 1003, "c4": 1004, "c5": 1005}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--form", choices=["plain", "precision"], default="plain")
+    ap.add_argument("--lbits", type=int, default=21)
+    ap.add_argument("--theta", type=float, default=0.7)
+    ap.add_argument("--bucket", type=int, default=16)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--persistent", action="store_true")
+    ap.add_argument("--error-samples", type=int, default=2048)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def make_inputs(ic, workload):
+    _, gen, n, _, _ = WORKLOADS[workload]
+    seed = SEEDS[workload]
+    if gen == "batch":
+        pm, vr, sizes = ic.plummer_batch(256, seed)
+        return pm, vr, [int(s) for s in sizes]
+    return getattr(ic, gen)(n, seed) + (None,)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+        else:
+            self.lines = []
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- ours --
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import astro_gb300 as ag
+    from astro_gb300 import ic
+    from astro_gb300 import layouts as L
+
+    torch.cuda.set_device(local)
+    desc, _, _, over, dt = WORKLOADS[args.workload]
+    pm, vr, sizes = make_inputs(ic, args.workload)
+    n = len(pm)
+    flags = L.FLAG_PERSISTENT if args.persistent else 0
+    form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
+                          bucket=args.bucket, block_warps=args.warps, flags=flags, form=form,
+                          **over)
+    nsys = len(sizes) if sizes else 1
+    sim = ag.Simulation(p, max_n=n, max_systems=nsys)
+    upload = (lambda: sim.upload_systems(pm, vr, sizes)) if sizes else (lambda: sim.upload(pm, vr))
+    upload()
+    stream = torch.cuda.ExternalStream(sim.stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    # Warm-up (also captures the step graph).
+    for _ in range(args.warmup):
+        sim.draw(dt, 1)
+    sim.synchronize()
+
+    # Timed region: K steps, each after an L2 flush, timed by CUDA events on
+    # the context's stream.
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                starts[k].record(stream)
+                sim.draw(dt, 1)
+                ends[k].record(stream)
+        sim.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_ms = sum(step_ms)
+    t_ms_max = reduce_max(t_ms, world)
+    value = n * args.steps * world / (t_ms_max * 1e-3)
+
+    # One instrumented step: per-stage times and the traversal's roofline.
+    stages = {}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    with torch.cuda.stream(stream):
+        flush.fill_(1)
+        ev[0].record(stream)
+        sim.generate_morton_codes()
+        ev[1].record(stream)
+        sim.sort()
+        ev[2].record(stream)
+        sim.build_tree()
+        ev[3].record(stream)
+        sim.barnes_hut()
+        ev[4].record(stream)
+        sim.update_spheres(dt)
+        ev[5].record(stream)
+    sim.synchronize()
+    for i, name in enumerate(["bbox+encode", "sort+reorder", "build", "traverse", "integrate"]):
+        stages[name] = ev[i].elapsed_time(ev[i + 1])
+    interactions, visits = sim.read_stats()
+    sizes_, offsets, counts = sim.tree_info()
+
+    # Traversal alone, several launches after a flush each, for the roofline.
+    trav_ms = []
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            sim.generate_morton_codes()
+            sim.sort()
+            sim.build_tree()
+            flush.fill_(2)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.barnes_hut()
+            e1.record(stream)
+            sim.update_spheres(0.0)
+        sim.synchronize()
+        trav_ms.append(e0.elapsed_time(e1))
+    trav = float(np.mean(trav_ms))
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peaks, peak_src = measured_peaks()
+    fp32_peak = 2 * 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    achieved = interactions * FLOPS_PER_INTERACTION / (trav * 1e-3) / 1e12
+
+    # Error against the FP64 direct sum on sampled particles (current state).
+    rng = np.random.default_rng(SEEDS[args.workload])
+    samples = np.sort(rng.choice(n, size=min(args.error_samples, n), replace=False)).astype(np.uint32)
+    sim.generate_morton_codes()
+    sim.sort()
+    sim.build_tree()
+    sim.barnes_hut()
+    acc = sim.read_accel()
+    direct = sim.direct_accel_f64(samples)
+    sim.update_spheres(0.0)
+    err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+
+    # End to end through the C ABI with pinned host buffers.
+    e2e = None
+    if not args.no_e2e:
+        pin_pm = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+        pin_vr = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+        hpm = pin_pm.numpy().view(L.POSITION_MASS)
+        hvr = pin_vr.numpy().view(L.VELOCITY_RADIUS)
+        hpm[:] = pm
+        hvr[:] = vr
+        up = ((lambda: sim.upload_systems(hpm, hvr, sizes)) if sizes
+              else (lambda: sim.upload(hpm, hvr)))
+        for _ in range(max(1, args.warmup)):
+            up()
+            sim.draw(dt, 1)
+            sim.download(hpm, hvr)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            up()
+            sim.draw(dt, 1)
+            sim.download(hpm, hvr)
+        te = time.perf_counter() - t0
+        te = reduce_max(te, world)
+        e2e = {"value": n * args.steps * world / te, "unit": UNIT,
+               "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 64 * n,
+               "ms_per_step": te * 1e3 / args.steps}
+
+    passes = (3 * args.lbits + (int(np.ceil(np.log2(nsys))) if nsys > 1 else 0) + 7) // 8
+    launches_per_step = 7 + passes + (args.lbits + 1)
+    sim.close()
+    return dict(n=n, desc=desc, dt=dt, p=p, value=value, t_ms=t_ms_max, wall=wall,
+                step_ms=step_ms, stages=stages, interactions=interactions, visits=visits,
+                counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
+                fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
+                launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr)
+
+
+# ----------------------------------------------------------- CPU side --
+
+def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
+    """The CPU restatement on all host cores: whole steps of the same
+    workload until the time budget is spent (at least one)."""
+    from oracle import oracle as orc
+
+    cores = orc.set_threads(0)
+    steps, t_total = 0, 0.0
+    pm_c, vr_c = pm.copy(), vr.copy()
+    while True:
+        t0 = time.perf_counter()
+        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+        t_total += time.perf_counter() - t0
+        steps += 1
+        if t_total >= budget_s:
+            break
+    return {"value": len(pm) * steps / t_total, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} whole step(s) of the same workload (N={len(pm)}), 64 one-bit "
+                      f"split passes per sort, {t_total:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement timed on the host cores."""
+    import astro_gb300 as ag
+    from astro_gb300 import ic
+    from astro_gb300 import layouts as L
+    from oracle import oracle as orc
+
+    desc, _, _, over, dt = WORKLOADS[args.workload]
+    pm, vr, sizes = make_inputs(ic, args.workload)
+    n = len(pm)
+    form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
+                          bucket=args.bucket, form=form, **over)
+    cores = orc.set_threads(0)
+    pm_c, vr_c = pm.copy(), vr.copy()
+    for _ in range(args.warmup):
+        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+    t = time.perf_counter() - t0
+    value = n * args.steps / t
+    sample = f"{args.steps} whole steps of the workload (N={n}), 64 one-bit split passes per sort"
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if form == 0 else "f32+f64",
+        "data": "synthetic (seeded, Philox4x32-10)", "impl": "reference",
+        "config": config_dict(args, desc, n, dt, p),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def config_dict(args, desc, n, dt, p):
+    return {"workload": f"{args.workload}: {desc}", "n": n, "preset": "PHYSICAL",
+            "form": args.form, "lbits": p.lbits, "theta": p.theta, "eps": p.softening,
+            "dt": dt, "bucket": p.bucket, "G": p.g,
+            "l2": "flushed (256 MB write) before every timed step",
+            "parallelism": "replicas (one independent system per GPU)"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)))
+        return 0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    r = run_ours(args, world, rank, local)
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            cpu = cpu_run(args, r["pm"], r["vr"], r["sizes"], r["p"], r["dt"], args.cpu_seconds)
+        line = {
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["t_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.form == "plain" else "f32+f64",
+            "data": "synthetic (seeded, Philox4x32-10)",
+            "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"]),
+            "e2e": r["e2e"], "gpu_launches": r["launches"],
+            "roofline": {"kernel": "traverse_phys_kernel", "bound": "fp32",
+                         "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
+                         "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
+                         "flops_per_launch": r["interactions"] * FLOPS_PER_INTERACTION,
+                         "launch_ms": r["trav_ms"],
+                         "peak_source": f"2 x 128 FP32 lanes x SMs x sm_max_mhz ({r['peak_src']} peaks file)"},
+            "cpu_baseline": cpu, "clocks": r["clocks"],
+            "error_vs_fp64_direct": {"median": float(np.median(r["err"])),
+                                     "p99": float(np.percentile(r["err"], 99)),
+                                     "samples": int(len(r["err"]))},
+            "interactions_per_particle": r["interactions"] / r["n"],
+            "node_visits_per_particle": r["visits"] / r["n"],
+            "stages_ms": r["stages"], "layer_counts": r["counts"],
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -80,6 +80,8 @@ struct PhysState {
     std::vector<float> sum32;    // Sx, Sy, Sz, M per node (plain)
     std::vector<double> sum64;   // Sx, Sy, Sz, M per node (precision)
     std::vector<uint32_t> pbeg, pend, cbeg, cend;
+    std::vector<float> quad;     // Qxx, Qyy, Qzz, Qxy, Qxz, Qyz per node (quadrupole flag)
+    std::vector<float> ncrit2;   // per-node opening radius^2 (delta flag)
     uint64_t interactions = 0, visits = 0;
 
     void layout(const uint32_t* sys_sizes) {
@@ -110,6 +112,8 @@ struct PhysState {
         pend.assign(capacity, 0);
         cbeg.assign(capacity, 0);
         cend.assign(capacity, 0);
+        quad.assign(6 * capacity, 0.0f);
+        ncrit2.assign(capacity, 0.0f);
     }
 
     // Bounding box, quantiser and opening thresholds per system.
@@ -364,8 +368,24 @@ struct PhysState {
                 const float* c = &cm[4ull * nd];
                 float dx = c[0] - px, dy = c[1] - py, dz = c[2] - pz;
                 float r2t = dx * dx + dy * dy + dz * dz;
-                if (r2t > crit2[l]) {
+                const float crit = (p.flags & 0x8u) ? ncrit2[nd] : crit2[l];
+                if (r2t > crit) {
                     add(dx, dy, dz, r2t, c[3]);
+                    if (p.flags & 0x10u) {
+                        const float* q = &quad[6ull * nd];
+                        float r2 = r2t + eps2;
+                        float inv = 1.0f / std::sqrt(r2);
+                        float inv2 = inv * inv, inv5 = inv2 * inv2 * inv;
+                        float inv7 = inv5 * inv2;
+                        float qx = q[0] * dx + q[3] * dy + q[4] * dz;
+                        float qy = q[3] * dx + q[1] * dy + q[5] * dz;
+                        float qz = q[4] * dx + q[5] * dy + q[2] * dz;
+                        float dqd = dx * qx + dy * qy + dz * qz;
+                        float w = 2.5f * dqd * inv7;
+                        ax += g * (w * dx - qx * inv5);
+                        ay += g * (w * dy - qy * inv5);
+                        az += g * (w * dz - qz * inv5);
+                    }
                 } else if (l == 0 || pend[nd] - pbeg[nd] <= bucket) {
                     for (uint32_t j = pbeg[nd]; j < pend[nd]; ++j) {
                         if (j == ip) continue;
@@ -403,12 +423,70 @@ struct PhysState {
             }
     }
 
+    // Quadrupole moments about each node's centre of mass (parallel-axis
+    // sums over children) and the delta-corrected opening radius
+    // (size / theta + |com - cell centre|)^2.
+    void moments() {
+        const bool want_q = (p.flags & 0x10u) != 0, want_d = (p.flags & 0x8u) != 0;
+        if (!want_q && !want_d) return;
+        for (uint32_t l = 0; l < layers; ++l) {
+            uint32_t off = offsets[l], u = counts[l];
+#pragma omp parallel for schedule(dynamic, 64)
+            for (int64_t kk = 0; kk < (int64_t)u; ++kk) {
+                uint32_t node = off + (uint32_t)kk;
+                const float* c = &cm[4ull * node];
+                float q[6] = {0, 0, 0, 0, 0, 0};
+                if (want_q) {
+                    auto add = [&](float m, float dx, float dy, float dz) {
+                        float r2 = dx * dx + dy * dy + dz * dz;
+                        q[0] += m * (3 * dx * dx - r2);
+                        q[1] += m * (3 * dy * dy - r2);
+                        q[2] += m * (3 * dz * dz - r2);
+                        q[3] += m * (3 * dx * dy);
+                        q[4] += m * (3 * dx * dz);
+                        q[5] += m * (3 * dy * dz);
+                    };
+                    if (l == 0) {
+                        for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
+                            const float* x = &rel[4ull * i];
+                            add(x[3], x[0] - c[0], x[1] - c[1], x[2] - c[2]);
+                        }
+                    } else {
+                        for (uint32_t ch = cbeg[node]; ch < cend[node]; ++ch) {
+                            const float* cc = &cm[4ull * ch];
+                            add(cc[3], cc[0] - c[0], cc[1] - c[1], cc[2] - c[2]);
+                            for (int a = 0; a < 6; ++a) q[a] += quad[6ull * ch + a];
+                        }
+                    }
+                    for (int a = 0; a < 6; ++a) quad[6ull * node + a] = q[a];
+                }
+                if (want_d) {
+                    uint32_t s = sys_of[pbeg[node]];
+                    uint64_t code = (sorted[pbeg[node]] & ((1ull << (3 * lbits)) - 1)) >> (3 * l);
+                    uint32_t cc[3] = {0, 0, 0};
+                    for (uint32_t b = 0; b < lbits - l; ++b)
+                        for (int a = 0; a < 3; ++a) cc[a] |= (uint32_t)((code >> (3 * b + a)) & 1) << b;
+                    float size = std::ldexp(quant[s].ext, (int)l - (int)lbits);
+                    float dd = 0;
+                    for (int a = 0; a < 3; ++a) {
+                        float center = quant[s].lo[a] + (float)(2 * cc[a] + 1) * (0.5f * size);
+                        float d = c[a] - center;
+                        dd += d * d;
+                    }
+                    float crit = size / p.theta + std::sqrt(dd);
+                    ncrit2[node] = crit * crit;
+                }
+            }
+        }
+    }
+
     void step(uint32_t split_passes, float dt) {
         setup_quant();
         encode();
         sort(split_passes);
         topology();
         aggregate();
+        moments();
         traverse_and_integrate(dt);
     }
 
