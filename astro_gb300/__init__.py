@@ -9,12 +9,13 @@ from . import layouts
 from ._native import AstroError, LIB_PATH
 from .layouts import (COLOR_TYPE, OCTREE_NODE, POSITION_MASS, VELOCITY_RADIUS, Params,
                       PRESET_PHYSICAL, PRESET_REFERENCE, FORM_PLAIN, FORM_PRECISION,
-                      FLAG_IEEE_EXACT, FLAG_NO_GRAPH, FLAG_PERSISTENT)
+                      FLAG_IEEE_EXACT, FLAG_NO_GRAPH, FLAG_PERSISTENT, FLAG_OPEN_DELTA,
+                      FLAG_QUADRUPOLE, FLAG_PER_PARTICLE)
 from .simulation import Simulation, default_params, version
 
 __all__ = [
     "AstroError", "LIB_PATH", "Simulation", "default_params", "version", "layouts", "Params",
     "POSITION_MASS", "VELOCITY_RADIUS", "COLOR_TYPE", "OCTREE_NODE", "PRESET_PHYSICAL",
     "PRESET_REFERENCE", "FORM_PLAIN", "FORM_PRECISION", "FLAG_IEEE_EXACT", "FLAG_NO_GRAPH",
-    "FLAG_PERSISTENT",
+    "FLAG_PERSISTENT", "FLAG_OPEN_DELTA", "FLAG_QUADRUPOLE", "FLAG_PER_PARTICLE",
 ]

@@ -321,6 +321,42 @@ __global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
 
 // -------------------------------------------------------- aggregation ----
 
+// Traceless quadrupole accumulation of mass m at offset d from the centre of
+// mass: Q += m (3 d d^T - |d|^2 I), components Qxx, Qyy, Qxy, Qxz, Qyz, each
+// product and sum rounded separately.
+__device__ __forceinline__ void quad_add(float q[5], float m, float dx, float dy, float dz) {
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const float tx = __fmul_rn(3.0f, dx), ty = __fmul_rn(3.0f, dy);
+    q[0] = __fadd_rn(q[0], __fmul_rn(m, __fsub_rn(__fmul_rn(tx, dx), r2)));
+    q[1] = __fadd_rn(q[1], __fmul_rn(m, __fsub_rn(__fmul_rn(ty, dy), r2)));
+    q[2] = __fadd_rn(q[2], __fmul_rn(m, __fmul_rn(tx, dy)));
+    q[3] = __fadd_rn(q[3], __fmul_rn(m, __fmul_rn(tx, dz)));
+    q[4] = __fadd_rn(q[4], __fmul_rn(m, __fmul_rn(ty, dz)));
+}
+
+// Opening radius^2 of a node: (size / theta + |com - cell centre|)^2, the
+// cell found from the node's key prefix in its system's box.
+__device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint32_t l, float4 cm) {
+    const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
+    const SysInfo& si = a.sys[s];
+    const uint64_t mask = (3u * a.lbits >= 64) ? ~0ull : ((1ull << (3u * a.lbits)) - 1ull);
+    const uint64_t code = (key & mask) >> (3u * l);
+    const float size = __fmul_rn(si.ext, exp2_exact((int)l - (int)a.lbits));
+    const float half = __fmul_rn(0.5f, size);
+    const float cx = __fadd_rn(si.lo[0], __fmul_rn((float)(2u * compact3_21(code) + 1u), half));
+    const float cy = __fadd_rn(si.lo[1], __fmul_rn((float)(2u * compact3_21(code >> 1) + 1u), half));
+    const float cz = __fadd_rn(si.lo[2], __fmul_rn((float)(2u * compact3_21(code >> 2) + 1u), half));
+    const float dx = __fsub_rn(cm.x, cx), dy = __fsub_rn(cm.y, cy), dz = __fsub_rn(cm.z, cz);
+    const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const float crit = __fadd_rn(__fdiv_rn(size, a.theta), __fsqrt_rn(dd));
+    return __fmul_rn(crit, crit);
+}
+
+__device__ __forceinline__ void emit_group(const AggArgs& a, uint32_t b, uint32_t e) {
+    const uint32_t slot = atomicAdd(a.group_count, 1u);
+    a.groups[slot] = make_uint2(b, e);
+}
+
 // aggregateLeafNodes (Octree.metal:53-117), one thread per leaf.
 // kMode 0 (REFERENCE): state in upload order, gathered through perm; FP32
 //   sums of m and x*m in sorted order; the last leaf sums [start, numUnique)
@@ -380,6 +416,21 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
     }
     a.node_cm[j] = cm;
     a.node_rng[j] = make_uint4(0u, 0u, pb, pe);
+    if (kMode != 0) {
+        if (a.want_quad) {
+            float q[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+            for (uint32_t i = pb; i < pe; ++i) {
+                const float4 x = a.pos[i];
+                quad_add(q, x.w, __fsub_rn(x.x, cm.x), __fsub_rn(x.y, cm.y), __fsub_rn(x.z, cm.z));
+            }
+            a.node_q[j] = make_float4(q[0], q[1], q[2], q[3]);
+            a.node_qyz[j] = q[4];
+        }
+        if (a.want_delta) a.node_crit2[j] = node_crit2(a, key, 0, cm);
+        // A leaf holding more than one group is cut into group-sized chunks.
+        if (pe - pb > kGroupSize)
+            for (uint32_t b = pb; b < pe; b += kGroupSize) emit_group(a, b, min(b + kGroupSize, pe));
+    }
 }
 
 // aggregateNodes (Octree.metal:120-202), one thread per node of layer l.
@@ -440,6 +491,52 @@ __global__ void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off, u
     }
     a.node_cm[node] = cm;
     a.node_rng[node] = make_uint4(cb, ce, pb, pe);
+    if (kMode != 0) {
+        if (a.want_quad) {
+            float q[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+            for (uint32_t c = cb; c < ce; ++c) {
+                const float4 cc = a.node_cm[c];
+                quad_add(q, cc.w, __fsub_rn(cc.x, cm.x), __fsub_rn(cc.y, cm.y), __fsub_rn(cc.z, cm.z));
+                const float4 qc = a.node_q[c];
+                q[0] = __fadd_rn(q[0], qc.x);
+                q[1] = __fadd_rn(q[1], qc.y);
+                q[2] = __fadd_rn(q[2], qc.z);
+                q[3] = __fadd_rn(q[3], qc.w);
+                q[4] = __fadd_rn(q[4], a.node_qyz[c]);
+            }
+            a.node_q[node] = make_float4(q[0], q[1], q[2], q[3]);
+            a.node_qyz[node] = q[4];
+        }
+        if (a.want_delta) a.node_crit2[node] = node_crit2(a, a.sorted_keys[pb], l, cm);
+        // Groups: a node over the group size packs runs of consecutive
+        // small children (greedy, in child order); a small top-layer node is
+        // a group by itself.
+        if (pe - pb > kGroupSize) {
+            uint32_t gb = 0, ge = 0;
+            for (uint32_t c = cb; c < ce; ++c) {
+                const uint4 rc = a.node_rng[c];
+                const uint32_t cc = rc.w - rc.z;
+                if (cc <= kGroupSize) {
+                    if (ge == gb) {
+                        gb = rc.z;
+                        ge = rc.w;
+                    } else if ((ge - gb) + cc <= kGroupSize) {
+                        ge = rc.w;
+                    } else {
+                        emit_group(a, gb, ge);
+                        gb = rc.z;
+                        ge = rc.w;
+                    }
+                } else if (ge != gb) {
+                    emit_group(a, gb, ge);
+                    gb = ge = 0;
+                }
+            }
+            if (ge != gb) emit_group(a, gb, ge);
+        } else if (l == a.lbits) {
+            emit_group(a, pb, pe);
+        }
+    }
 }
 
 // ---------------------------------------------------------- integrate ----

@@ -35,9 +35,20 @@ struct AggArgs {
     uint4* node_rng;
     uint64_t* node_key;
     void* node_sum;
+    // PHYSICAL extras: quadrupole moments, per-node opening radius, groups.
+    float* node_crit2;
+    float4* node_q;        // Qxx, Qyy, Qxy, Qxz
+    float* node_qyz;       // Qyz
+    uint2* groups;         // particle ranges of the group walk
+    uint32_t* group_count;
     uint32_t n;
     uint32_t lbits;
+    uint32_t want_quad;
+    uint32_t want_delta;
+    float theta;
 };
+
+constexpr uint32_t kGroupSize = 32;  // particles per group walk (one warp)
 
 struct DirectArgs {
     const float4* pos;
@@ -85,6 +96,17 @@ struct TraverseArgs {
     uint32_t* err;
     unsigned long long* stats;
     uint32_t* queue;
+    // PHYSICAL opening radius / quadrupole / group walk.
+    uint32_t delta;
+    uint32_t quad;
+    const float* node_crit2;
+    const float4* node_q;
+    const float* node_qyz;
+    const uint2* groups;
+    const uint32_t* group_count;
+    uint32_t* frontier;       // per-warp ping-pong buffers, 2 * frontier_cap each
+    uint32_t frontier_cap;
+    uint32_t nsys;
 };
 
 cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,
@@ -137,8 +159,13 @@ struct TraverseConfig {
     bool batched;     // several systems: per-lane system and root
     bool persistent;  // persistent blocks with a work-stealing chunk queue
     int warps;        // warps per block (2, 4 or 8)
+    bool quad;        // quadrupole terms (group walk template switch)
 };
 cudaError_t launch_traverse_ref(const TraverseArgs& a, cudaStream_t st);
 cudaError_t launch_traverse_phys(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
+// Group walk: warps resident in the persistent launch (sizes the frontier
+// scratch) and the launch itself.
+uint32_t group_walk_warps(const TraverseConfig& c);
+cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
 
 }  // namespace astro

@@ -25,6 +25,17 @@ __host__ __device__ __forceinline__ uint64_t spread3_21(uint32_t v) {
     return x;
 }
 
+// Inverse of spread3_21: gather bits 0, 3, 6, ... of x into bits 0, 1, 2, ...
+__host__ __device__ __forceinline__ uint32_t compact3_21(uint64_t x) {
+    x &= 0x1249249249249249ull;
+    x = (x ^ (x >> 2)) & 0x10C30C30C30C30C3ull;
+    x = (x ^ (x >> 4)) & 0x100F00F00F00F00Full;
+    x = (x ^ (x >> 8)) & 0x001F0000FF0000FFull;
+    x = (x ^ (x >> 16)) & 0x001F00000000FFFFull;
+    x = (x ^ (x >> 32)) & 0x00000000001FFFFFull;
+    return (uint32_t)x;
+}
+
 __host__ __device__ __forceinline__ uint64_t interleave3(uint32_t x, uint32_t y, uint32_t z) {
     return spread3_21(x) | (spread3_21(y) << 1) | (spread3_21(z) << 2);
 }
@@ -70,6 +81,7 @@ enum DeviceError : uint32_t {
     kErrLookbackTimeout = 1u << 0,  // a decoupled look-back wait gave up
     kErrStackOverflow = 1u << 1,    // a traversal stack bound was hit
     kErrBadLayer = 1u << 2,
+    kErrFrontier = 1u << 3,         // a group walk's frontier exceeded its buffer
 };
 
 // Bounded spin for decoupled look-back: after this many polls the waiting

@@ -116,8 +116,14 @@ int ensure_tree(astro_ctx* ctx, uint64_t capacity) {
     ctx->node_sum = nullptr;
     dev_free(ctx->node_pbeg);
     dev_free(ctx->node_cbeg);
+    dev_free(ctx->node_crit2);
+    dev_free(ctx->node_q);
+    dev_free(ctx->node_qyz);
     ctx->tree_capacity = 0;
     const uint64_t cap = capacity;
+    CK(dev_alloc(&ctx->node_crit2, cap));
+    CK(dev_alloc(&ctx->node_q, cap));
+    CK(dev_alloc(&ctx->node_qyz, cap));
     CK(dev_alloc(&ctx->node_cm, cap));
     CK(dev_alloc(&ctx->node_rng, cap));
     CK(dev_alloc(&ctx->node_key, cap));
@@ -144,6 +150,8 @@ int check_device(astro_ctx* ctx) {
         CK(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
         if (err & astro::kErrLookbackTimeout)
             return fail(ctx, ASTRO_ERR_DEVICE_TIMEOUT, "a decoupled look-back wait gave up");
+        if (err & astro::kErrFrontier)
+            return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW, "a group walk frontier exceeded its buffer");
         return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW, "a traversal stack bound was hit");
     }
     return ASTRO_OK;
@@ -169,7 +177,26 @@ astro::TraverseConfig traverse_config(const astro_ctx* ctx) {
     c.batched = ctx->nsys > 1;
     c.persistent = (ctx->p.flags & ASTRO_FLAG_PERSISTENT) != 0;
     c.warps = ctx->p.block_warps ? (int)ctx->p.block_warps : 4;
+    c.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) != 0;
     return c;
+}
+
+bool group_walk(const astro_ctx* ctx) {
+    return is_phys(ctx) && (ctx->p.flags & ASTRO_FLAG_PER_PARTICLE) == 0;
+}
+
+// Frontier scratch of the group walk: two buffers of frontier_cap node
+// indices per resident warp of the persistent launch.
+int ensure_frontier(astro_ctx* ctx) {
+    if (!group_walk(ctx)) return ASTRO_OK;
+    astro::TraverseConfig c = traverse_config(ctx);
+    const size_t words = (size_t)astro::group_walk_warps(c) * 2 * ctx->frontier_cap;
+    if (words <= ctx->frontier_words) return ASTRO_OK;
+    dev_free(ctx->frontier);
+    ctx->frontier_words = 0;
+    CK(dev_alloc(&ctx->frontier, words));
+    ctx->frontier_words = words;
+    return ASTRO_OK;
 }
 
 // --------------------------------------------------------------- stages --
@@ -240,8 +267,17 @@ int stage_build(astro_ctx* ctx) {
     a.node_rng = ctx->node_rng;
     a.node_key = ctx->node_key;
     a.node_sum = ctx->node_sum;
+    a.node_crit2 = ctx->node_crit2;
+    a.node_q = ctx->node_q;
+    a.node_qyz = ctx->node_qyz;
+    a.groups = ctx->groups;
+    a.group_count = ctx->counters + 2;
     a.n = count;
     a.lbits = ctx->lbits;
+    a.want_quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
+    a.want_delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
+    a.theta = ctx->p.theta;
+    CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
     const int mode = !is_phys(ctx) ? 0 : (is_prec(ctx) ? 2 : 1);
     CK(astro::launch_aggregate(mode, a, ctx->layers, st));
     ctx->tree_valid = true;
@@ -269,6 +305,16 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     a.err = ctx->err;
     a.stats = ctx->stats;
     a.queue = ctx->counters + 1;
+    a.delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
+    a.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
+    a.node_crit2 = ctx->node_crit2;
+    a.node_q = ctx->node_q;
+    a.node_qyz = ctx->node_qyz;
+    a.groups = ctx->groups;
+    a.group_count = ctx->counters + 2;
+    a.frontier = ctx->frontier;
+    a.frontier_cap = ctx->frontier_cap;
+    a.nsys = ctx->nsys;
     if (is_phys(ctx)) {
         a.eps2 = ctx->p.softening * ctx->p.softening;
         a.pos = ctx->pos[1];
@@ -304,7 +350,13 @@ int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
     }
     if (!ctx->state_in_b || !ctx->tree_valid)
         return fail(ctx, ASTRO_ERR_STATE, "traverse called before sort and build");
-    CK(astro::launch_traverse_phys(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
+    if (group_walk(ctx)) {
+        int r = ensure_frontier(ctx);
+        if (r != ASTRO_OK) return r;
+        CK(astro::launch_traverse_groups(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
+    } else {
+        CK(astro::launch_traverse_phys(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
+    }
     ctx->state_in_b = false;
     return ASTRO_OK;
 }
@@ -407,6 +459,7 @@ int astro_params_default(uint32_t preset, astro_params* out) {
         out->damping = 1.0f;
         out->type_accel_scale[0] = out->type_accel_scale[1] = out->type_accel_scale[2] = 1.0f;
         out->bucket = 16;
+        out->flags = ASTRO_FLAG_OPEN_DELTA | ASTRO_FLAG_QUADRUPOLE;
     } else {
         return ASTRO_ERR_INVALID_ARGUMENT;
     }
@@ -456,6 +509,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     ctx->topo_lookback_words = (size_t)astro::topology_tiles(max_n) * 32 + 32;
     CKC(dev_alloc(&ctx->topo_lookback, ctx->topo_lookback_words));
     CKC(dev_alloc(&ctx->counters, 16));
+    CKC(dev_alloc(&ctx->groups, max_n));
     CKC(dev_alloc(&ctx->err, 1));
     CKC(dev_alloc(&ctx->stats, 2));
     CKC(dev_alloc(&ctx->layer_count, ASTRO_MAX_LAYERS));
@@ -506,6 +560,11 @@ int astro_destroy(astro_ctx* ctx) {
     if (ctx->node_sum) cudaFree(ctx->node_sum);
     dev_free(ctx->node_pbeg);
     dev_free(ctx->node_cbeg);
+    dev_free(ctx->node_crit2);
+    dev_free(ctx->node_q);
+    dev_free(ctx->node_qyz);
+    dev_free(ctx->groups);
+    dev_free(ctx->frontier);
     if (ctx->readback) cudaFree(ctx->readback);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -530,6 +589,7 @@ int astro_set_params(astro_ctx* ctx, const astro_params* params) {
     if (params->form == ASTRO_FORM_PRECISION && (r = ensure_x64(ctx)) != ASTRO_OK) return r;
     ctx->p = *params;
     drop_graph(ctx);
+    if ((r = ensure_frontier(ctx)) != ASTRO_OK) return r;
     if (structural) {
         ctx->uploaded = false;
         ctx->tree_valid = false;
@@ -558,6 +618,7 @@ static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityR
     layer_table(sizes, ctx->lbits, &ctx->layers, &ctx->capacity);
     int r = ensure_tree(ctx, ctx->capacity);
     if (r != ASTRO_OK) return r;
+    if ((r = ensure_frontier(ctx)) != ASTRO_OK) return r;
     if (prec && (r = ensure_x64(ctx)) != ASTRO_OK) return r;
     // Systems and chunks.
     std::vector<SysInfo> sys(ctx->nsys);

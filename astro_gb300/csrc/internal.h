@@ -99,6 +99,13 @@ struct astro_ctx {
     void* node_sum = nullptr;         // float4 or double4 raw sums (S, M)
     uint32_t* node_pbeg = nullptr;
     uint32_t* node_cbeg = nullptr;
+    float* node_crit2 = nullptr;      // opening radius^2 per node
+    float4* node_q = nullptr;         // quadrupole Qxx, Qyy, Qxy, Qxz
+    float* node_qyz = nullptr;        // quadrupole Qyz
+    uint2* groups = nullptr;          // group-walk particle ranges (<= n)
+    uint32_t* frontier = nullptr;     // group-walk per-warp frontier buffers
+    size_t frontier_words = 0;
+    uint32_t frontier_cap = 16384;
     uint32_t* layer_count = nullptr;  // device [ASTRO_MAX_LAYERS]
 
     // Systems.
@@ -113,7 +120,7 @@ struct astro_ctx {
     size_t sort_temp_bytes = 0;
     uint32_t* topo_lookback = nullptr;
     size_t topo_lookback_words = 0;
-    uint32_t* counters = nullptr;             // [0] topology tiles, [1] traversal queue
+    uint32_t* counters = nullptr;             // [0] topology tiles, [1] traversal queue, [2] groups
     uint32_t* err = nullptr;                  // device error word
     unsigned long long* stats = nullptr;      // interactions, node visits
     void* readback = nullptr;

@@ -88,7 +88,79 @@ __global__ __launch_bounds__(128) void traverse_ref_kernel(TraverseArgs a) {
     atomicAdd(&a.stats[1], (unsigned long long)visits);
 }
 
-// One softened interaction of the PHYSICAL preset: a += G m d / (r^2 + eps^2)^(3/2).
+// Interaction terms of the PHYSICAL preset (G = g):
+//   particle / monopole:  t = G m d / (r^2 + eps^2)^(3/2)
+//   quadrupole addition:  t += G [ 5/2 (d.Qd) d / r^7 - Qd / r^5 ]
+// with d the displacement towards the source and Q traceless
+// (Qzz = -Qxx - Qyy). kExact rounds every operation separately, in the
+// order of the CPU restatement; otherwise rsqrt and FMAs are used.
+template <bool kExact>
+__device__ __forceinline__ void cell_term(float dx, float dy, float dz, float r2t, float m,
+                                          bool quad, float4 q, float qyz, float g, float eps2,
+                                          float& tx, float& ty, float& tz) {
+    if (kExact) {
+        const float r2 = __fadd_rn(r2t, eps2);
+        const float inv = __fdiv_rn(1.0f, __fsqrt_rn(r2));
+        const float inv2 = __fmul_rn(inv, inv);
+        const float inv3 = __fmul_rn(inv2, inv);
+        const float sc = __fmul_rn(__fmul_rn(g, m), inv3);
+        tx = __fmul_rn(dx, sc);
+        ty = __fmul_rn(dy, sc);
+        tz = __fmul_rn(dz, sc);
+        if (quad) {
+            const float inv5 = __fmul_rn(inv3, inv2), inv7 = __fmul_rn(inv5, inv2);
+            const float qzz = -__fadd_rn(q.x, q.y);
+            const float qx = __fadd_rn(__fadd_rn(__fmul_rn(q.x, dx), __fmul_rn(q.z, dy)), __fmul_rn(q.w, dz));
+            const float qy = __fadd_rn(__fadd_rn(__fmul_rn(q.z, dx), __fmul_rn(q.y, dy)), __fmul_rn(qyz, dz));
+            const float qz = __fadd_rn(__fadd_rn(__fmul_rn(q.w, dx), __fmul_rn(qyz, dy)), __fmul_rn(qzz, dz));
+            const float dqd = __fadd_rn(__fadd_rn(__fmul_rn(dx, qx), __fmul_rn(dy, qy)), __fmul_rn(dz, qz));
+            const float w = __fmul_rn(__fmul_rn(2.5f, dqd), inv7);
+            tx = __fadd_rn(tx, __fmul_rn(g, __fsub_rn(__fmul_rn(w, dx), __fmul_rn(qx, inv5))));
+            ty = __fadd_rn(ty, __fmul_rn(g, __fsub_rn(__fmul_rn(w, dy), __fmul_rn(qy, inv5))));
+            tz = __fadd_rn(tz, __fmul_rn(g, __fsub_rn(__fmul_rn(w, dz), __fmul_rn(qz, inv5))));
+        }
+    } else {
+        const float inv = rsqrtf(r2t + eps2);
+        const float inv2 = inv * inv;
+        const float inv3 = inv2 * inv;
+        const float sc = g * m * inv3;
+        tx = dx * sc;
+        ty = dy * sc;
+        tz = dz * sc;
+        if (quad) {
+            const float inv5 = inv3 * inv2, inv7 = inv5 * inv2;
+            const float qzz = -(q.x + q.y);
+            const float qx = fmaf(q.x, dx, fmaf(q.z, dy, q.w * dz));
+            const float qy = fmaf(q.z, dx, fmaf(q.y, dy, qyz * dz));
+            const float qz = fmaf(q.w, dx, fmaf(qyz, dy, qzz * dz));
+            const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+            const float w = 2.5f * dqd * inv7;
+            const float gi5 = g * inv5, gw = g * w;
+            tx = fmaf(gw, dx, fmaf(-gi5, qx, tx));
+            ty = fmaf(gw, dy, fmaf(-gi5, qy, ty));
+            tz = fmaf(gw, dz, fmaf(-gi5, qz, tz));
+        }
+    }
+}
+
+template <bool kExact>
+__device__ __forceinline__ void particle_term(float dx, float dy, float dz, float m, float g,
+                                              float eps2, float& tx, float& ty, float& tz) {
+    if (kExact) {
+        const float r2t =
+            __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        cell_term<true>(dx, dy, dz, r2t, m, false, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, g, eps2,
+                        tx, ty, tz);
+    } else {
+        const float inv = rsqrtf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2))));
+        const float sc = g * m * (inv * inv * inv);
+        tx = dx * sc;
+        ty = dy * sc;
+        tz = dz * sc;
+    }
+}
+
+// Per-lane acceleration sum: plain or compensated (Kahan) per component.
 template <bool kExact, bool kKahan>
 struct Accum {
     float ax = 0.f, ay = 0.f, az = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
@@ -110,53 +182,10 @@ struct Accum {
             s = kExact ? __fadd_rn(s, t) : s + t;
         }
     }
-
-    // r2t = |d|^2 computed by the caller with separately rounded operations.
-    __device__ __forceinline__ void monopole(float dx, float dy, float dz, float r2t, float m,
-                                             float g, float eps2) {
-        float sc;
-        if (kExact) {
-            const float r2 = __fadd_rn(r2t, eps2);
-            const float inv = __fdiv_rn(1.0f, __fsqrt_rn(r2));
-            sc = __fmul_rn(__fmul_rn(g, m), __fmul_rn(__fmul_rn(inv, inv), inv));
-            add1(ax, cx, __fmul_rn(dx, sc));
-            add1(ay, cy, __fmul_rn(dy, sc));
-            add1(az, cz, __fmul_rn(dz, sc));
-        } else {
-            const float inv = rsqrtf(r2t + eps2);
-            sc = (g * m) * (inv * inv * inv);
-            if (kKahan) {
-                add1(ax, cx, dx * sc);
-                add1(ay, cy, dy * sc);
-                add1(az, cz, dz * sc);
-            } else {
-                ax = fmaf(dx, sc, ax);
-                ay = fmaf(dy, sc, ay);
-                az = fmaf(dz, sc, az);
-            }
-        }
-    }
-
-    __device__ __forceinline__ void particle(float dx, float dy, float dz, float m, float g,
-                                             float eps2) {
-        if (kExact) {
-            const float r2t =
-                __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            monopole(dx, dy, dz, r2t, m, g, eps2);
-        } else {
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-            const float inv = rsqrtf(r2);
-            const float sc = (g * m) * (inv * inv * inv);
-            if (kKahan) {
-                add1(ax, cx, dx * sc);
-                add1(ay, cy, dy * sc);
-                add1(az, cz, dz * sc);
-            } else {
-                ax = fmaf(dx, sc, ax);
-                ay = fmaf(dy, sc, ay);
-                az = fmaf(dz, sc, az);
-            }
-        }
+    __device__ __forceinline__ void add(float tx, float ty, float tz) {
+        add1(ax, cx, tx);
+        add1(ay, cy, ty);
+        add1(az, cz, tz);
     }
 };
 
@@ -226,9 +255,18 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
                         dz = __fsub_rn(c.z, me.z);
             const float r2t =
                 __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            const bool accept = active && r2t > __ldg(&crit2[layer]);
+            const float crit = a.delta ? __ldg(&a.node_crit2[nd]) : __ldg(&crit2[layer]);
+            const bool accept = active && r2t > crit;
             if (accept) {
-                acc.monopole(dx, dy, dz, r2t, c.w, g, eps2);
+                float tx, ty, tz;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                float qyz = 0.f;
+                if (a.quad) {
+                    q = __ldg(&a.node_q[nd]);
+                    qyz = __ldg(&a.node_qyz[nd]);
+                }
+                cell_term<kExact>(dx, dy, dz, r2t, c.w, a.quad != 0, q, qyz, g, eps2, tx, ty, tz);
+                acc.add(tx, ty, tz);
                 ++inter;
             }
             visits += active ? 1u : 0u;
@@ -258,9 +296,12 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
                     if (open) {
                         for (uint32_t q = 0; q < cnt; ++q) {
                             const float4 p = s_tile[warp][q];
-                            if (t + q != ip)
-                                acc.particle(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
-                                             __fsub_rn(p.z, me.z), p.w, g, eps2);
+                            if (t + q != ip) {
+                                float tx, ty, tz;
+                                particle_term<kExact>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
+                                                      __fsub_rn(p.z, me.z), p.w, g, eps2, tx, ty, tz);
+                                acc.add(tx, ty, tz);
+                            }
                         }
                         inter += cnt - ((ip - t) < cnt ? 1u : 0u);
                     }
@@ -319,6 +360,234 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
     (void)lt;
 }
 
+
+// Group walk. One warp per group of <= 32 consecutive sorted particles (a
+// tree cell or a pack of sibling cells, built with the tree). The warp walks
+// the tree breadth first from the system's root, testing 32 frontier nodes
+// at a time against the group's bounding box: accepted nodes go to the cell
+// list (records staged in shared memory), opened leaves and buckets to the
+// leaf list, other opened nodes put their children in the next frontier
+// (per-warp buffers in global memory). Lists are evaluated by all lanes,
+// one particle per lane, whenever they fill and at the end: cells into one
+// sum, leaf particles (32 at a time through shared memory) into another.
+constexpr int kCellCap = 64;
+constexpr int kLeafCap = 32;
+
+template <bool kExact, bool kPrec, bool kQuad, int kWarps>
+__global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArgs a) {
+    __shared__ float4 s_cm[kWarps][kCellCap];
+    __shared__ float4 s_q[kWarps][kQuad ? kCellCap : 1];
+    __shared__ float s_qyz[kWarps][kQuad ? kCellCap : 1];
+    __shared__ uint2 s_leaf[kWarps][kLeafCap];
+    __shared__ float4 s_tile[kWarps][32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t gw = blockIdx.x * kWarps + warp;
+    uint32_t* buf0 = a.frontier + (size_t)gw * 2 * a.frontier_cap;
+    uint32_t* buf1 = buf0 + a.frontier_cap;
+    const uint32_t ngroups = *a.group_count;
+    const float g = a.g, eps2 = a.eps2;
+    uint32_t inter = 0, visits = 0;
+
+    while (true) {
+        uint32_t gi = 0;
+        if (lane == 0) gi = atomicAdd(a.queue, 1u);
+        gi = __shfl_sync(kFullMask, gi, 0);
+        if (gi >= ngroups) break;
+        const uint2 gr = a.groups[gi];
+        const uint32_t gcount = gr.y - gr.x;
+        const bool valid = lane < gcount;
+        const uint32_t ip = gr.x + lane;
+        const float4 me = valid ? a.pos[ip] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t sys = a.nsys > 1 ? (uint32_t)(a.sorted_keys[gr.x] >> (3u * a.lbits)) : 0u;
+        const float* crit_layer = a.sys[sys].crit2;
+        // Group bounding box.
+        float lo_x = valid ? me.x : INFINITY, lo_y = valid ? me.y : INFINITY,
+              lo_z = valid ? me.z : INFINITY;
+        float hi_x = valid ? me.x : -INFINITY, hi_y = valid ? me.y : -INFINITY,
+              hi_z = valid ? me.z : -INFINITY;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo_x = fminf(lo_x, __shfl_xor_sync(kFullMask, lo_x, o));
+            lo_y = fminf(lo_y, __shfl_xor_sync(kFullMask, lo_y, o));
+            lo_z = fminf(lo_z, __shfl_xor_sync(kFullMask, lo_z, o));
+            hi_x = fmaxf(hi_x, __shfl_xor_sync(kFullMask, hi_x, o));
+            hi_y = fmaxf(hi_y, __shfl_xor_sync(kFullMask, hi_y, o));
+            hi_z = fmaxf(hi_z, __shfl_xor_sync(kFullMask, hi_z, o));
+        }
+        Accum<kExact, kPrec> cells, leaves;
+        uint32_t n_cell = 0, n_leaf = 0;
+
+        auto flush_cells = [&]() {
+            __syncwarp();
+            if (valid) {
+                for (uint32_t e = 0; e < n_cell; ++e) {
+                    const float4 c = s_cm[warp][e];
+                    const float dx = __fsub_rn(c.x, me.x), dy = __fsub_rn(c.y, me.y),
+                                dz = __fsub_rn(c.z, me.z);
+                    const float r2t = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                         __fmul_rn(dz, dz))
+                                             : fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    float tx, ty, tz;
+                    if (kQuad)
+                        cell_term<kExact>(dx, dy, dz, r2t, c.w, true, s_q[warp][e], s_qyz[warp][e], g,
+                                          eps2, tx, ty, tz);
+                    else
+                        cell_term<kExact>(dx, dy, dz, r2t, c.w, false, make_float4(0.f, 0.f, 0.f, 0.f),
+                                          0.f, g, eps2, tx, ty, tz);
+                    cells.add(tx, ty, tz);
+                }
+                inter += n_cell;
+            }
+            __syncwarp();
+            n_cell = 0;
+        };
+        auto flush_leaves = [&]() {
+            for (uint32_t e = 0; e < n_leaf; ++e) {
+                const uint2 rg = s_leaf[warp][e];
+                for (uint32_t t = rg.x; t < rg.y; t += 32u) {
+                    const uint32_t j = t + lane;
+                    __syncwarp();
+                    if (j < rg.y) s_tile[warp][lane] = __ldg(&a.pos[j]);
+                    __syncwarp();
+                    const uint32_t cnt = min(32u, rg.y - t);
+                    if (valid) {
+                        for (uint32_t q = 0; q < cnt; ++q) {
+                            const float4 p = s_tile[warp][q];
+                            if (t + q != ip) {
+                                float tx, ty, tz;
+                                particle_term<kExact>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
+                                                      __fsub_rn(p.z, me.z), p.w, g, eps2, tx, ty, tz);
+                                leaves.add(tx, ty, tz);
+                            }
+                        }
+                        inter += cnt - ((ip - t) < cnt ? 1u : 0u);
+                    }
+                }
+            }
+            __syncwarp();
+            n_leaf = 0;
+        };
+
+        uint32_t* cur = buf0;
+        uint32_t* nxt = buf1;
+        if (lane == 0) cur[0] = a.sys[sys].root;
+        uint32_t ncur = 1;
+        int layer = (int)a.lbits;
+        __syncwarp();
+        while (ncur > 0) {
+            uint32_t nnext = 0;
+            for (uint32_t base = 0; base < ncur; base += 32u) {
+                const uint32_t k = base + lane;
+                const bool has = k < ncur;
+                const uint32_t nd = has ? cur[k] : 0u;
+                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+                uint4 r = make_uint4(0u, 0u, 0u, 0u);
+                float crit = 0.f;
+                if (has) {
+                    c = __ldg(&a.node_cm[nd]);
+                    r = __ldg(&a.node_rng[nd]);
+                    crit = a.delta ? __ldg(&a.node_crit2[nd]) : __ldg(&crit_layer[layer]);
+                }
+                const float bx = fmaxf(fmaxf(__fsub_rn(lo_x, c.x), __fsub_rn(c.x, hi_x)), 0.f);
+                const float by = fmaxf(fmaxf(__fsub_rn(lo_y, c.y), __fsub_rn(c.y, hi_y)), 0.f);
+                const float bz = fmaxf(fmaxf(__fsub_rn(lo_z, c.z), __fsub_rn(c.z, hi_z)), 0.f);
+                const float dist2 =
+                    __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
+                const bool acc = has && dist2 > crit;
+                const bool leaf = has && !acc && (layer == 0 || r.w - r.z <= a.bucket);
+                const bool opn = has && !acc && !leaf;
+                const uint32_t tested = __popc(__ballot_sync(kFullMask, has));
+                if (valid) visits += tested;
+                // Accepted cells, in frontier order.
+                const uint32_t bacc = __ballot_sync(kFullMask, acc);
+                if (bacc) {
+                    if (n_cell + __popc(bacc) > (uint32_t)kCellCap) flush_cells();
+                    if (acc) {
+                        const uint32_t slot = n_cell + __popc(bacc & lt);
+                        s_cm[warp][slot] = c;
+                        if (kQuad) {
+                            s_q[warp][slot] = __ldg(&a.node_q[nd]);
+                            s_qyz[warp][slot] = __ldg(&a.node_qyz[nd]);
+                        }
+                    }
+                    n_cell += __popc(bacc);
+                }
+                // Opened leaves and buckets, in frontier order.
+                const uint32_t bleaf = __ballot_sync(kFullMask, leaf);
+                if (bleaf) {
+                    if (n_leaf + __popc(bleaf) > (uint32_t)kLeafCap) flush_leaves();
+                    if (leaf) s_leaf[warp][n_leaf + __popc(bleaf & lt)] = make_uint2(r.z, r.w);
+                    n_leaf += __popc(bleaf);
+                }
+                // Children of opened nodes form the next frontier, in order.
+                const uint32_t cnt = opn ? r.y - r.x : 0u;
+                uint32_t incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                    if (lane >= (uint32_t)o) incl += y;
+                }
+                const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+                if (nnext + total <= a.frontier_cap) {
+                    const uint32_t o0 = nnext + incl - cnt;
+                    for (uint32_t j = 0; j < cnt; ++j) nxt[o0 + j] = r.x + j;
+                    nnext += total;
+                } else if (lane == 0) {
+                    atomicOr(a.err, kErrFrontier);
+                }
+            }
+            __syncwarp();
+            uint32_t* t = cur;
+            cur = nxt;
+            nxt = t;
+            ncur = nnext;
+            --layer;
+        }
+        flush_cells();
+        flush_leaves();
+
+        if (valid) {
+            const float cl = a.clampv, dt = a.dt;
+            const float sx = kExact ? __fadd_rn(cells.ax, leaves.ax) : cells.ax + leaves.ax;
+            const float sy = kExact ? __fadd_rn(cells.ay, leaves.ay) : cells.ay + leaves.ay;
+            const float sz = kExact ? __fadd_rn(cells.az, leaves.az) : cells.az + leaves.az;
+            const float ax = fminf(fmaxf(sx, -cl), cl);
+            const float ay = fminf(fmaxf(sy, -cl), cl);
+            const float az = fminf(fmaxf(sz, -cl), cl);
+            a.acc[ip] = make_float4(ax, ay, az, 0.f);
+            float4 v = a.vel_in[ip];
+            v.x = __fadd_rn(v.x, __fmul_rn(ax, dt));
+            v.y = __fadd_rn(v.y, __fmul_rn(ay, dt));
+            v.z = __fadd_rn(v.z, __fmul_rn(az, dt));
+            a.vel_out[ip] = v;
+            a.id_out[ip] = a.id_in[ip];
+            if (kPrec) {
+                const size_t n = a.n;
+                const double ddt = (double)dt;
+                a.x64_out[ip] = __dadd_rn(a.x64_in[ip], __dmul_rn((double)v.x, ddt));
+                a.x64_out[n + ip] = __dadd_rn(a.x64_in[n + ip], __dmul_rn((double)v.y, ddt));
+                a.x64_out[2 * n + ip] = __dadd_rn(a.x64_in[2 * n + ip], __dmul_rn((double)v.z, ddt));
+                a.pos_out[ip] = me;
+            } else {
+                a.pos_out[ip] = make_float4(__fadd_rn(me.x, __fmul_rn(v.x, dt)),
+                                            __fadd_rn(me.y, __fmul_rn(v.y, dt)),
+                                            __fadd_rn(me.z, __fmul_rn(v.z, dt)), me.w);
+            }
+        }
+    }
+    unsigned long long i64 = inter, v64 = visits;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        i64 += __shfl_xor_sync(kFullMask, i64, o);
+        v64 += __shfl_xor_sync(kFullMask, v64, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], i64);
+        atomicAdd(&a.stats[1], v64);
+    }
+}
+
 namespace {
 
 int sm_count() {
@@ -373,7 +642,59 @@ cudaError_t launch_phys_b(const TraverseArgs& a, const TraverseConfig& c, cudaSt
                      : launch_phys_p<kExact, kPrec, false>(a, c, st);
 }
 
+template <bool kExact, bool kPrec, bool kQuad, int kWarps>
+uint32_t group_blocks() {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, traverse_group_kernel<kExact, kPrec, kQuad, kWarps>, kWarps * 32, 0);
+    return (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
+}
+
+template <bool kExact, bool kPrec, bool kQuad, int kWarps>
+cudaError_t launch_group_t(const TraverseArgs& a, cudaStream_t st) {
+    const uint32_t blocks = group_blocks<kExact, kPrec, kQuad, kWarps>();
+    cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    traverse_group_kernel<kExact, kPrec, kQuad, kWarps><<<blocks, kWarps * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool kExact, bool kPrec, bool kQuad>
+cudaError_t launch_group_w(const TraverseArgs& a, int warps, cudaStream_t st) {
+    return warps == 8 ? launch_group_t<kExact, kPrec, kQuad, 8>(a, st)
+                      : launch_group_t<kExact, kPrec, kQuad, 4>(a, st);
+}
+
+template <bool kExact, bool kPrec>
+cudaError_t launch_group_q(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st) {
+    return c.quad ? launch_group_w<kExact, kPrec, true>(a, c.warps, st)
+                  : launch_group_w<kExact, kPrec, false>(a, c.warps, st);
+}
+
 }  // namespace
+
+uint32_t group_walk_warps(const TraverseConfig& c) {
+    // Warps of the persistent launch of the instantiation this config selects.
+    uint32_t blocks;
+    const bool w8 = c.warps == 8;
+#define ASTRO_GB(E, P, Q) (w8 ? group_blocks<E, P, Q, 8>() : group_blocks<E, P, Q, 4>())
+    if (c.exact) {
+        if (c.precision) blocks = c.quad ? ASTRO_GB(true, true, true) : ASTRO_GB(true, true, false);
+        else blocks = c.quad ? ASTRO_GB(true, false, true) : ASTRO_GB(true, false, false);
+    } else {
+        if (c.precision) blocks = c.quad ? ASTRO_GB(false, true, true) : ASTRO_GB(false, true, false);
+        else blocks = c.quad ? ASTRO_GB(false, false, true) : ASTRO_GB(false, false, false);
+    }
+#undef ASTRO_GB
+    return blocks * (w8 ? 8u : 4u);
+}
+
+cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    if (c.exact)
+        return c.precision ? launch_group_q<true, true>(a, c, st) : launch_group_q<true, false>(a, c, st);
+    return c.precision ? launch_group_q<false, true>(a, c, st) : launch_group_q<false, false>(a, c, st);
+}
 
 cudaError_t launch_traverse_ref(const TraverseArgs& a, cudaStream_t st) {
     if (a.n == 0) return cudaSuccess;

@@ -22,6 +22,9 @@ FORM_PRECISION = 1
 FLAG_IEEE_EXACT = 0x1
 FLAG_NO_GRAPH = 0x2
 FLAG_PERSISTENT = 0x4
+FLAG_OPEN_DELTA = 0x8
+FLAG_QUADRUPOLE = 0x10
+FLAG_PER_PARTICLE = 0x20
 
 IC_PLUMMER = 0
 IC_DISK_BULGE = 1

@@ -119,7 +119,11 @@ typedef enum astro_preset {
     ASTRO_PRESET_REFERENCE = 0,
     /* Physical units: bounding-box quantiser, geometric cell size, G and
      * Plummer softening eps^2, particle-particle interaction inside opened
-     * leaves and buckets, leapfrog kick-drift-kick. */
+     * leaves and buckets, and updateSpheres' kick-drift without damping
+     * (leapfrog with velocities at half steps). Defaults add the quadrupole
+     * term and the delta-corrected opening radius, and walk the tree once per
+     * group of <= 32 particles (ASTRO_FLAG_PER_PARTICLE restores per-particle
+     * decisions). */
     ASTRO_PRESET_PHYSICAL = 1
 } astro_preset;
 
@@ -136,8 +140,15 @@ typedef enum astro_form {
                                        reproduces the CPU restatement bit for bit) */
 #define ASTRO_FLAG_NO_GRAPH   0x2u  /* astro_step launches kernels directly
                                        instead of replaying a CUDA graph */
-#define ASTRO_FLAG_PERSISTENT 0x4u  /* traversal runs as a persistent kernel
-                                       with a work-stealing chunk queue */
+#define ASTRO_FLAG_PERSISTENT 0x4u  /* per-particle traversal runs as a persistent
+                                       kernel with a work-stealing chunk queue */
+#define ASTRO_FLAG_OPEN_DELTA 0x8u  /* PHYSICAL: open a node unless the distance
+                                       exceeds size/theta + |com - cell centre| */
+#define ASTRO_FLAG_QUADRUPOLE 0x10u /* PHYSICAL: accepted nodes add their
+                                       traceless quadrupole term */
+#define ASTRO_FLAG_PER_PARTICLE 0x20u /* PHYSICAL: decide node by node for each
+                                       particle (the reference's walk) instead of
+                                       the group walk over <= 32-particle groups */
 
 typedef struct astro_params {
     uint32_t preset;          /* astro_preset */
@@ -202,9 +213,11 @@ int astro_build(astro_ctx* ctx);     /* countUniqueMortonCodes + aggregateLeafNo
 int astro_traverse(astro_ctx* ctx);  /* barnesHut (BarnesHut.metal:22-101) */
 int astro_integrate(astro_ctx* ctx, float dt); /* updateSpheres (BarnesHut.metal:169-196) */
 
-/* nsteps full steps. REFERENCE: encode, sort, build, traverse, integrate.
- * PHYSICAL: kick(dt/2)+drift(dt), encode, sort, build, traverse+kick(dt/2),
- * with one extra force evaluation the first time after an upload. */
+/* nsteps full steps: encode, sort, build, traverse, integrate (v += a dt,
+ * x += v dt). PHYSICAL fuses the integration into the traversal and keeps
+ * the particle state in Morton order between steps. The step is captured in
+ * a CUDA graph once per upload/params/dt and replayed (ASTRO_FLAG_NO_GRAPH
+ * launches it directly). */
 int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps);
 int astro_synchronize(astro_ctx* ctx);
 

@@ -80,7 +80,7 @@ struct PhysState {
     std::vector<float> sum32;    // Sx, Sy, Sz, M per node (plain)
     std::vector<double> sum64;   // Sx, Sy, Sz, M per node (precision)
     std::vector<uint32_t> pbeg, pend, cbeg, cend;
-    std::vector<float> quad;     // Qxx, Qyy, Qzz, Qxy, Qxz, Qyz per node (quadrupole flag)
+    std::vector<float> quad;     // Qxx, Qyy, Qxy, Qxz, Qyz per node (quadrupole flag)
     std::vector<float> ncrit2;   // per-node opening radius^2 (delta flag)
     uint64_t interactions = 0, visits = 0;
 
@@ -112,7 +112,7 @@ struct PhysState {
         pend.assign(capacity, 0);
         cbeg.assign(capacity, 0);
         cend.assign(capacity, 0);
-        quad.assign(6 * capacity, 0.0f);
+        quad.assign(5 * capacity, 0.0f);
         ncrit2.assign(capacity, 0.0f);
     }
 
@@ -322,42 +322,81 @@ struct PhysState {
         }
     }
 
-    // barnesHut (BarnesHut.metal:22-101) per particle in sorted order, then
-    // the fused kick-drift. Children are pushed in order and popped last
-    // first, as the reference's stack does.
-    void traverse_and_integrate(float dt) {
-        const float g = p.g, eps2 = p.softening * p.softening, clampv = p.force_clamp;
-        const uint32_t bucket = p.bucket;
-        const bool kahan = prec;
+    static constexpr uint32_t kFlagDelta = 0x8u;      // ASTRO_FLAG_OPEN_DELTA
+    static constexpr uint32_t kFlagQuad = 0x10u;      // ASTRO_FLAG_QUADRUPOLE
+    static constexpr uint32_t kFlagPerParticle = 0x20u;  // ASTRO_FLAG_PER_PARTICLE
+    static constexpr uint32_t kGroup = 32;            // particles per group walk
+
+    // One accumulator (plain or Kahan) per component.
+    struct Acc {
+        float s[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+        void add(bool kahan, const float t[3]) {
+            for (int a = 0; a < 3; ++a) {
+                if (kahan) {
+                    float y = t[a] - c[a];
+                    float u = s[a] + y;
+                    c[a] = (u - s[a]) - y;
+                    s[a] = u;
+                } else {
+                    s[a] += t[a];
+                }
+            }
+        }
+    };
+
+    // Softened monopole of mass m at displacement d (r2t = |d|^2), plus the
+    // quadrupole term of q = {Qxx, Qyy, Qxy, Qxz, Qyz} (Qzz = -Qxx - Qyy)
+    // when q is not NULL:
+    //   a = G m d / r^3 + G [ 5/2 (d.Qd) d / r^7 - Qd / r^5 ],  r^2 = |d|^2 + eps^2.
+    void term(float dx, float dy, float dz, float r2t, float m, const float* q, float out[3]) const {
+        const float g = p.g, eps2 = p.softening * p.softening;
+        float r2 = r2t + eps2;
+        float inv = 1.0f / std::sqrt(r2);
+        float inv2 = inv * inv;
+        float inv3 = inv2 * inv;
+        float sc = (g * m) * inv3;
+        out[0] = dx * sc;
+        out[1] = dy * sc;
+        out[2] = dz * sc;
+        if (q) {
+            float inv5 = inv3 * inv2, inv7 = inv5 * inv2;
+            float qzz = -(q[0] + q[1]);
+            float qx = (q[0] * dx + q[2] * dy) + q[3] * dz;
+            float qy = (q[2] * dx + q[1] * dy) + q[4] * dz;
+            float qz = (q[3] * dx + q[4] * dy) + qzz * dz;
+            float dqd = (dx * qx + dy * qy) + dz * qz;
+            float w = (2.5f * dqd) * inv7;
+            out[0] = out[0] + g * ((w * dx) - (qx * inv5));
+            out[1] = out[1] + g * ((w * dy) - (qy * inv5));
+            out[2] = out[2] + g * ((w * dz) - (qz * inv5));
+        }
+    }
+
+    float node_crit2(uint32_t nd, uint32_t l, uint32_t s) const {
+        return (p.flags & kFlagDelta) ? ncrit2[nd] : quant[s].crit2[l];
+    }
+
+    void finish(uint32_t ip, const float a[3]) {
+        const float cl = p.force_clamp;
+        float* o = &acc[4ull * ip];
+        for (int k = 0; k < 3; ++k) o[k] = std::fmin(std::fmax(a[k], -cl), cl);
+        o[3] = 0.0f;
+    }
+
+    // barnesHut (BarnesHut.metal:22-101) per particle in sorted order:
+    // children pushed in order and popped last first, as the reference's
+    // stack does; one accumulator in visiting order.
+    void traverse_per_particle() {
+        const bool kahan = prec, quad_on = (p.flags & kFlagQuad) != 0;
         uint64_t tot_inter = 0, tot_visits = 0;
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : tot_inter, tot_visits)
         for (int64_t ipp = 0; ipp < (int64_t)n; ++ipp) {
             uint32_t ip = (uint32_t)ipp, s = sys_of[ip];
-            const float* crit2 = quant[s].crit2;
             const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
-            float ax = 0, ay = 0, az = 0, cx = 0, cy = 0, cz = 0;
+            Acc A;
+            float t[3];
             uint64_t inter = 0, vis = 0;
-            auto add = [&](float dx, float dy, float dz, float r2t, float m) {
-                float r2 = r2t + eps2;
-                float inv = 1.0f / std::sqrt(r2);
-                float inv3 = (inv * inv) * inv;
-                float sc = (g * m) * inv3;
-                float tx = dx * sc, ty = dy * sc, tz = dz * sc;
-                if (kahan) {
-                    float y, t;
-                    y = tx - cx; t = ax + y; cx = (t - ax) - y; ax = t;
-                    y = ty - cy; t = ay + y; cy = (t - ay) - y; ay = t;
-                    y = tz - cz; t = az + y; cz = (t - az) - y; az = t;
-                } else {
-                    ax += tx;
-                    ay += ty;
-                    az += tz;
-                }
-                ++inter;
-            };
             std::vector<uint32_t> st_node, st_layer;
-            st_node.reserve(8 * layers + 8);
-            st_layer.reserve(8 * layers + 8);
             st_node.push_back(offsets[lbits] + s);
             st_layer.push_back(lbits);
             while (!st_node.empty()) {
@@ -368,30 +407,18 @@ struct PhysState {
                 const float* c = &cm[4ull * nd];
                 float dx = c[0] - px, dy = c[1] - py, dz = c[2] - pz;
                 float r2t = dx * dx + dy * dy + dz * dz;
-                const float crit = (p.flags & 0x8u) ? ncrit2[nd] : crit2[l];
-                if (r2t > crit) {
-                    add(dx, dy, dz, r2t, c[3]);
-                    if (p.flags & 0x10u) {
-                        const float* q = &quad[6ull * nd];
-                        float r2 = r2t + eps2;
-                        float inv = 1.0f / std::sqrt(r2);
-                        float inv2 = inv * inv, inv5 = inv2 * inv2 * inv;
-                        float inv7 = inv5 * inv2;
-                        float qx = q[0] * dx + q[3] * dy + q[4] * dz;
-                        float qy = q[3] * dx + q[1] * dy + q[5] * dz;
-                        float qz = q[4] * dx + q[5] * dy + q[2] * dz;
-                        float dqd = dx * qx + dy * qy + dz * qz;
-                        float w = 2.5f * dqd * inv7;
-                        ax += g * (w * dx - qx * inv5);
-                        ay += g * (w * dy - qy * inv5);
-                        az += g * (w * dz - qz * inv5);
-                    }
-                } else if (l == 0 || pend[nd] - pbeg[nd] <= bucket) {
+                if (r2t > node_crit2(nd, l, s)) {
+                    term(dx, dy, dz, r2t, c[3], quad_on ? &quad[5ull * nd] : nullptr, t);
+                    A.add(kahan, t);
+                    ++inter;
+                } else if (l == 0 || pend[nd] - pbeg[nd] <= p.bucket) {
                     for (uint32_t j = pbeg[nd]; j < pend[nd]; ++j) {
                         if (j == ip) continue;
                         const float* q = &rel[4ull * j];
                         float ex = q[0] - px, ey = q[1] - py, ez = q[2] - pz;
-                        add(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3]);
+                        term(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3], nullptr, t);
+                        A.add(kahan, t);
+                        ++inter;
                     }
                 } else {
                     for (uint32_t ch = cbeg[nd]; ch < cend[nd]; ++ch) {
@@ -400,17 +427,133 @@ struct PhysState {
                     }
                 }
             }
-            float* o = &acc[4ull * ip];
-            o[0] = std::fmin(std::fmax(ax, -clampv), clampv);
-            o[1] = std::fmin(std::fmax(ay, -clampv), clampv);
-            o[2] = std::fmin(std::fmax(az, -clampv), clampv);
-            o[3] = 0.0f;
+            finish(ip, A.s);
             tot_inter += inter;
             tot_visits += vis;
         }
         interactions = tot_inter;
         visits = tot_visits;
-        // Kick-drift (BarnesHut.metal:189-194 without damping and type scale).
+    }
+
+    // Groups for the group walk: every particle in exactly one group of at
+    // most kGroup consecutive (sorted) particles of one system.
+    //  - a node with more than kGroup particles packs its consecutive small
+    //    children (at most kGroup particles each) greedily, in child order;
+    //  - a top-layer node with at most kGroup particles is a group;
+    //  - a leaf with more than kGroup particles is cut into kGroup chunks.
+    std::vector<std::pair<uint32_t, uint32_t>> make_groups() const {
+        std::vector<std::pair<uint32_t, uint32_t>> groups;
+        for (uint32_t l = 0; l < layers; ++l)
+            for (uint32_t k = 0; k < counts[l]; ++k) {
+                uint32_t node = offsets[l] + k, pc = pend[node] - pbeg[node];
+                if (pc <= kGroup) {
+                    if (l == lbits) groups.push_back({pbeg[node], pend[node]});
+                    continue;
+                }
+                if (l == 0) {
+                    for (uint32_t b = pbeg[node]; b < pend[node]; b += kGroup)
+                        groups.push_back({b, std::min(b + kGroup, pend[node])});
+                    continue;
+                }
+                uint32_t gb = 0, ge = 0;
+                for (uint32_t ch = cbeg[node]; ch < cend[node]; ++ch) {
+                    uint32_t cc = pend[ch] - pbeg[ch];
+                    if (cc <= kGroup) {
+                        if (ge == gb) {
+                            gb = pbeg[ch];
+                            ge = pend[ch];
+                        } else if ((ge - gb) + cc <= kGroup) {
+                            ge = pend[ch];
+                        } else {
+                            groups.push_back({gb, ge});
+                            gb = pbeg[ch];
+                            ge = pend[ch];
+                        }
+                    } else if (ge != gb) {
+                        groups.push_back({gb, ge});
+                        gb = ge = 0;
+                    }
+                }
+                if (ge != gb) groups.push_back({gb, ge});
+            }
+        return groups;
+    }
+
+    // Group walk: the tree is walked once per group, breadth first from the
+    // system's root, against the group's bounding box. A node is accepted
+    // when the box lies outside its opening radius; an opened leaf or bucket
+    // goes to the particle list; other opened nodes contribute their
+    // children to the next level. Each particle then sums the accepted cells
+    // (in walk order) and, separately, the particles of the listed leaves and
+    // buckets (in walk order, itself excluded); a = cells + particles.
+    void traverse_groups() {
+        const bool kahan = prec, quad_on = (p.flags & kFlagQuad) != 0;
+        const auto groups = make_groups();
+        uint64_t tot_inter = 0, tot_visits = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot_inter, tot_visits)
+        for (int64_t gi = 0; gi < (int64_t)groups.size(); ++gi) {
+            const uint32_t gb = groups[gi].first, ge = groups[gi].second;
+            const uint32_t s = sys_of[gb];
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (uint32_t i = gb; i < ge; ++i)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], rel[4ull * i + a]);
+                    hi[a] = std::max(hi[a], rel[4ull * i + a]);
+                }
+            std::vector<uint32_t> frontier{offsets[lbits] + s}, next, cells, leaves;
+            uint64_t tested = 0;
+            for (int l = (int)lbits; !frontier.empty(); --l) {
+                next.clear();
+                for (uint32_t nd : frontier) {
+                    ++tested;
+                    const float* c = &cm[4ull * nd];
+                    float d[3];
+                    for (int a = 0; a < 3; ++a) d[a] = std::max(std::max(lo[a] - c[a], c[a] - hi[a]), 0.0f);
+                    float dist2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                    if (dist2 > node_crit2(nd, (uint32_t)l, s)) {
+                        cells.push_back(nd);
+                    } else if (l == 0 || pend[nd] - pbeg[nd] <= p.bucket) {
+                        leaves.push_back(nd);
+                    } else {
+                        for (uint32_t ch = cbeg[nd]; ch < cend[nd]; ++ch) next.push_back(ch);
+                    }
+                }
+                frontier.swap(next);
+            }
+            for (uint32_t ip = gb; ip < ge; ++ip) {
+                const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
+                Acc A, B;
+                float t[3];
+                uint64_t inter = 0;
+                for (uint32_t nd : cells) {
+                    const float* c = &cm[4ull * nd];
+                    float dx = c[0] - px, dy = c[1] - py, dz = c[2] - pz;
+                    term(dx, dy, dz, dx * dx + dy * dy + dz * dz, c[3],
+                         quad_on ? &quad[5ull * nd] : nullptr, t);
+                    A.add(kahan, t);
+                    ++inter;
+                }
+                for (uint32_t nd : leaves)
+                    for (uint32_t j = pbeg[nd]; j < pend[nd]; ++j) {
+                        if (j == ip) continue;
+                        const float* q = &rel[4ull * j];
+                        float ex = q[0] - px, ey = q[1] - py, ez = q[2] - pz;
+                        term(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3], nullptr, t);
+                        B.add(kahan, t);
+                        ++inter;
+                    }
+                float a3[3] = {A.s[0] + B.s[0], A.s[1] + B.s[1], A.s[2] + B.s[2]};
+                finish(ip, a3);
+                tot_inter += inter;
+                tot_visits += tested;
+            }
+        }
+        interactions = tot_inter;
+        visits = tot_visits;
+    }
+
+    // Kick-drift (BarnesHut.metal:189-194 without damping and type scale).
+    void integrate(float dt) {
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < (int64_t)n; ++i)
             for (int a = 0; a < 3; ++a) {
@@ -424,10 +567,10 @@ struct PhysState {
     }
 
     // Quadrupole moments about each node's centre of mass (parallel-axis
-    // sums over children) and the delta-corrected opening radius
-    // (size / theta + |com - cell centre|)^2.
+    // sums over children, traceless: Qzz = -Qxx - Qyy) and the
+    // delta-corrected opening radius (size / theta + |com - cell centre|)^2.
     void moments() {
-        const bool want_q = (p.flags & 0x10u) != 0, want_d = (p.flags & 0x8u) != 0;
+        const bool want_q = (p.flags & kFlagQuad) != 0, want_d = (p.flags & kFlagDelta) != 0;
         if (!want_q && !want_d) return;
         for (uint32_t l = 0; l < layers; ++l) {
             uint32_t off = offsets[l], u = counts[l];
@@ -435,16 +578,15 @@ struct PhysState {
             for (int64_t kk = 0; kk < (int64_t)u; ++kk) {
                 uint32_t node = off + (uint32_t)kk;
                 const float* c = &cm[4ull * node];
-                float q[6] = {0, 0, 0, 0, 0, 0};
                 if (want_q) {
+                    float q[5] = {0, 0, 0, 0, 0};
                     auto add = [&](float m, float dx, float dy, float dz) {
                         float r2 = dx * dx + dy * dy + dz * dz;
                         q[0] += m * (3 * dx * dx - r2);
                         q[1] += m * (3 * dy * dy - r2);
-                        q[2] += m * (3 * dz * dz - r2);
-                        q[3] += m * (3 * dx * dy);
-                        q[4] += m * (3 * dx * dz);
-                        q[5] += m * (3 * dy * dz);
+                        q[2] += m * (3 * dx * dy);
+                        q[3] += m * (3 * dx * dz);
+                        q[4] += m * (3 * dy * dz);
                     };
                     if (l == 0) {
                         for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
@@ -455,10 +597,10 @@ struct PhysState {
                         for (uint32_t ch = cbeg[node]; ch < cend[node]; ++ch) {
                             const float* cc = &cm[4ull * ch];
                             add(cc[3], cc[0] - c[0], cc[1] - c[1], cc[2] - c[2]);
-                            for (int a = 0; a < 6; ++a) q[a] += quad[6ull * ch + a];
+                            for (int a = 0; a < 5; ++a) q[a] += quad[5ull * ch + a];
                         }
                     }
-                    for (int a = 0; a < 6; ++a) quad[6ull * node + a] = q[a];
+                    for (int a = 0; a < 5; ++a) quad[5ull * node + a] = q[a];
                 }
                 if (want_d) {
                     uint32_t s = sys_of[pbeg[node]];
@@ -467,12 +609,13 @@ struct PhysState {
                     for (uint32_t b = 0; b < lbits - l; ++b)
                         for (int a = 0; a < 3; ++a) cc[a] |= (uint32_t)((code >> (3 * b + a)) & 1) << b;
                     float size = std::ldexp(quant[s].ext, (int)l - (int)lbits);
-                    float dd = 0;
+                    float half = 0.5f * size;
+                    float d[3];
                     for (int a = 0; a < 3; ++a) {
-                        float center = quant[s].lo[a] + (float)(2 * cc[a] + 1) * (0.5f * size);
-                        float d = c[a] - center;
-                        dd += d * d;
+                        float center = quant[s].lo[a] + (float)(2 * cc[a] + 1) * half;
+                        d[a] = c[a] - center;
                     }
+                    float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                     float crit = size / p.theta + std::sqrt(dd);
                     ncrit2[node] = crit * crit;
                 }
@@ -487,7 +630,9 @@ struct PhysState {
         topology();
         aggregate();
         moments();
-        traverse_and_integrate(dt);
+        if (p.flags & kFlagPerParticle) traverse_per_particle();
+        else traverse_groups();
+        integrate(dt);
     }
 
     void write_outputs(oracle_outputs* out) {

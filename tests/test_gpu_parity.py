@@ -145,12 +145,22 @@ def test_reference_plummer_all_in_tree(ag, oracle):
 
 # ------------------------------------------------------------- PHYSICAL --
 
-@pytest.mark.parametrize("lbits", [6, 10, 21])
-def test_physical_exact_bit_exact(ag, oracle, lbits):
+WALKS = {
+    "group": lambda L: L.FLAG_OPEN_DELTA | L.FLAG_QUADRUPOLE,
+    "group-monopole": lambda L: 0,
+    "particle": lambda L: L.FLAG_PER_PARTICLE | L.FLAG_OPEN_DELTA | L.FLAG_QUADRUPOLE,
+    "particle-monopole": lambda L: L.FLAG_PER_PARTICLE,
+}
+
+
+@pytest.mark.parametrize("walk,lbits", [("group", 6), ("group", 10), ("group", 21),
+                                        ("group-monopole", 21), ("particle", 21),
+                                        ("particle-monopole", 6)])
+def test_physical_exact_bit_exact(ag, oracle, walk, lbits):
     from astro_gb300 import ic
 
     L = ag.layouts
-    p = ag.default_params(L.PRESET_PHYSICAL, lbits=lbits, flags=L.FLAG_IEEE_EXACT)
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=lbits, flags=WALKS[walk](L) | L.FLAG_IEEE_EXACT)
     pm, vr = ic.plummer(16384, seed=1001)
     out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=3)
     pm_o, vr_o = pm.copy(), vr.copy()
@@ -161,13 +171,17 @@ def test_physical_exact_bit_exact(ag, oracle, lbits):
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
 
 
-@pytest.mark.parametrize("warps,persistent", [(4, False), (2, True), (8, False)])
-def test_physical_fast_within_tolerance(ag, oracle, warps, persistent):
+@pytest.mark.parametrize("walk,warps,persistent", [("group", 4, False), ("group", 8, False),
+                                                   ("group-monopole", 4, False),
+                                                   ("particle", 4, False), ("particle", 2, True),
+                                                   ("particle-monopole", 8, False)])
+def test_physical_fast_within_tolerance(ag, oracle, walk, warps, persistent):
     from astro_gb300 import ic
 
     L = ag.layouts
-    flags = L.FLAG_PERSISTENT if persistent else 0
-    p = ag.default_params(L.PRESET_PHYSICAL, flags=flags, block_warps=warps, softening=0.005)
+    flags = WALKS[walk](L) | (L.FLAG_PERSISTENT if persistent else 0)
+    p = ag.default_params(L.PRESET_PHYSICAL, flags=flags, block_warps=warps, softening=0.005,
+                          lbits=21)
     pm, vr = ic.disk_bulge(32768, seed=1002)
     out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=1)
     ref = oracle.phys_run(p, pm.copy(), vr.copy(), dt=5e-4, steps=1)
@@ -181,8 +195,8 @@ def test_physical_precision_form_bit_exact(ag, oracle):
     from astro_gb300 import ic
 
     L = ag.layouts
-    p = ag.default_params(L.PRESET_PHYSICAL, form=L.FORM_PRECISION, flags=L.FLAG_IEEE_EXACT,
-                          softening=0.002, lbits=10)
+    p = ag.default_params(L.PRESET_PHYSICAL, form=L.FORM_PRECISION,
+                          flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT, softening=0.002, lbits=10)
     pm, vr = ic.two_plummer(16384, seed=1003)
     out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=3)
     pm_o, vr_o = pm.copy(), vr.copy()
@@ -192,8 +206,9 @@ def test_physical_precision_form_bit_exact(ag, oracle):
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
 
 
-@pytest.mark.parametrize("persistent", [False, True])
-def test_physical_batched_bit_exact(ag, oracle, persistent):
+@pytest.mark.parametrize("walk,persistent", [("group", False), ("particle", False),
+                                             ("particle-monopole", True)])
+def test_physical_batched_bit_exact(ag, oracle, walk, persistent):
     from astro_gb300 import ic
 
     L = ag.layouts
@@ -201,7 +216,7 @@ def test_physical_batched_bit_exact(ag, oracle, persistent):
     parts = [ic.plummer(s, seed=1004, a=0.5 + 0.1 * k, system=k) for k, s in enumerate(sizes)]
     pm = np.concatenate([a for a, _ in parts])
     vr = np.concatenate([b for _, b in parts])
-    flags = L.FLAG_IEEE_EXACT | (L.FLAG_PERSISTENT if persistent else 0)
+    flags = WALKS[walk](L) | L.FLAG_IEEE_EXACT | (L.FLAG_PERSISTENT if persistent else 0)
     p = ag.default_params(L.PRESET_PHYSICAL, flags=flags)
     out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2, sizes=sizes)
     pm_o, vr_o = pm.copy(), vr.copy()
