@@ -57,7 +57,8 @@ SIGNATURES = {
                                      c_uint32]),
     "astro_read_nodes": (c_int, [c_void_p, c_void_p, c_uint64, c_uint64]),
     "astro_read_accel": (c_int, [c_void_p, c_void_p, c_uint32]),
-    "astro_read_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
+    "astro_read_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64),
+                                 POINTER(c_uint64)]),
     "astro_direct_accel_f64": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "astro_get_stream": (c_int, [c_void_p, POINTER(c_void_p)]),
     "astro_last_error": (c_char_p, [c_void_p]),

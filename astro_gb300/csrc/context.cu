@@ -338,7 +338,7 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
 // evaluates forces (the state is copied back to A unchanged).
 int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
     cudaStream_t st = ctx->stream;
-    CK(cudaMemsetAsync(ctx->stats, 0, 2 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->stats, 0, 3 * sizeof(unsigned long long), st));
     if (!is_phys(ctx)) {
         if (ctx->n_tree == 0) {
             CK(cudaMemsetAsync(ctx->acc, 0, sizeof(float4) * ctx->n, st));
@@ -511,7 +511,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     CKC(dev_alloc(&ctx->counters, 16));
     CKC(dev_alloc(&ctx->groups, max_n));
     CKC(dev_alloc(&ctx->err, 1));
-    CKC(dev_alloc(&ctx->stats, 2));
+    CKC(dev_alloc(&ctx->stats, 3));
     CKC(dev_alloc(&ctx->layer_count, ASTRO_MAX_LAYERS));
     CKC(dev_alloc(&ctx->sys, max_systems));
     CKC(dev_alloc(&ctx->bbox32, 6ull * max_systems));
@@ -520,7 +520,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     CKC(dev_alloc(&ctx->chunks, ctx->chunk_capacity));
     CKC(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
     CKC(cudaMemset(ctx->layer_count, 0, sizeof(uint32_t) * ASTRO_MAX_LAYERS));
-    CKC(cudaMemset(ctx->stats, 0, 2 * sizeof(unsigned long long)));
+    CKC(cudaMemset(ctx->stats, 0, 3 * sizeof(unsigned long long)));
     if (params->form == ASTRO_FORM_PRECISION && ensure_x64(ctx) != ASTRO_OK)
         return cleanup(ASTRO_ERR_OUT_OF_MEMORY);
 #undef CKC
@@ -871,13 +871,15 @@ int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n) {
     return check_device(ctx);
 }
 
-int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits) {
+int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits,
+                     uint64_t* cell_interactions) {
     NEED_UPLOAD();
-    unsigned long long s[2] = {0, 0};
+    unsigned long long s[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(s, ctx->stats, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
     int r = check_device(ctx);
     if (interactions) *interactions = s[0];
     if (node_visits) *node_visits = s[1];
+    if (cell_interactions) *cell_interactions = s[2];
     return r;
 }
 

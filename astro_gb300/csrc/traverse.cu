@@ -86,6 +86,7 @@ __global__ __launch_bounds__(128) void traverse_ref_kernel(TraverseArgs a) {
                              fminf(fmaxf(fz, -cl), cl), 0.f);
     atomicAdd(&a.stats[0], (unsigned long long)inter);
     atomicAdd(&a.stats[1], (unsigned long long)visits);
+    atomicAdd(&a.stats[2], (unsigned long long)inter);
 }
 
 // Interaction terms of the PHYSICAL preset (G = g):
@@ -197,7 +198,7 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
     const uint32_t lt = lanemask_lt();
     const uint32_t nchunks = (a.n + 31u) / 32u;
     const float g = a.g, eps2 = a.eps2;
-    uint32_t inter = 0, visits = 0;
+    uint32_t inter = 0, visits = 0, cell_inter = 0;
     uint32_t chunk = blockIdx.x * kWarps + warp;
     while (true) {
         if (kPersistent) {
@@ -268,6 +269,7 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
                 cell_term<kExact>(dx, dy, dz, r2t, c.w, a.quad != 0, q, qyz, g, eps2, tx, ty, tz);
                 acc.add(tx, ty, tz);
                 ++inter;
+                ++cell_inter;
             }
             visits += active ? 1u : 0u;
             const uint32_t open_mask = __ballot_sync(kFullMask, active && !accept);
@@ -347,15 +349,17 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
         if (!kPersistent) break;
     }
     // Statistics: one atomic per warp.
-    unsigned long long i64 = inter, v64 = visits;
+    unsigned long long i64 = inter, v64 = visits, c64 = cell_inter;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         i64 += __shfl_xor_sync(kFullMask, i64, o);
         v64 += __shfl_xor_sync(kFullMask, v64, o);
+        c64 += __shfl_xor_sync(kFullMask, c64, o);
     }
     if (lane == 0) {
         atomicAdd(&a.stats[0], i64);
         atomicAdd(&a.stats[1], v64);
+        atomicAdd(&a.stats[2], c64);
     }
     (void)lt;
 }
@@ -376,10 +380,11 @@ constexpr int kLeafCap = 32;
 template <bool kExact, bool kPrec, bool kQuad, int kWarps>
 __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArgs a) {
     __shared__ float4 s_cm[kWarps][kCellCap];
-    __shared__ float4 s_q[kWarps][kQuad ? kCellCap : 1];
-    __shared__ float s_qyz[kWarps][kQuad ? kCellCap : 1];
+    __shared__ float4 s_q[kWarps][kQuad ? kCellCap : 1];   // Qxx, Qyy, Qxy, Qxz
+    __shared__ float2 s_q2[kWarps][kQuad ? kCellCap : 1];  // Qyz, Qzz
     __shared__ uint2 s_leaf[kWarps][kLeafCap];
     __shared__ float4 s_tile[kWarps][32];
+    __shared__ uint32_t s_jdx[kWarps][32];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
     const uint32_t gw = blockIdx.x * kWarps + warp;
@@ -387,7 +392,7 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
     uint32_t* buf1 = buf0 + a.frontier_cap;
     const uint32_t ngroups = *a.group_count;
     const float g = a.g, eps2 = a.eps2;
-    uint32_t inter = 0, visits = 0;
+    uint32_t inter = 0, visits = 0, cell_inter = 0;
 
     while (true) {
         uint32_t gi = 0;
@@ -418,50 +423,134 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
         Accum<kExact, kPrec> cells, leaves;
         uint32_t n_cell = 0, n_leaf = 0;
 
+        // Cell list: every lane sums its particle against each staged cell.
+        // The fast path leaves G out of the terms and applies it once at the end.
         auto flush_cells = [&]() {
             __syncwarp();
             if (valid) {
-                for (uint32_t e = 0; e < n_cell; ++e) {
-                    const float4 c = s_cm[warp][e];
-                    const float dx = __fsub_rn(c.x, me.x), dy = __fsub_rn(c.y, me.y),
-                                dz = __fsub_rn(c.z, me.z);
-                    const float r2t = kExact ? __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
-                                                         __fmul_rn(dz, dz))
-                                             : fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    float tx, ty, tz;
-                    if (kQuad)
-                        cell_term<kExact>(dx, dy, dz, r2t, c.w, true, s_q[warp][e], s_qyz[warp][e], g,
-                                          eps2, tx, ty, tz);
-                    else
-                        cell_term<kExact>(dx, dy, dz, r2t, c.w, false, make_float4(0.f, 0.f, 0.f, 0.f),
-                                          0.f, g, eps2, tx, ty, tz);
-                    cells.add(tx, ty, tz);
+                if (kExact) {
+                    for (uint32_t e = 0; e < n_cell; ++e) {
+                        const float4 c = s_cm[warp][e];
+                        const float dx = __fsub_rn(c.x, me.x), dy = __fsub_rn(c.y, me.y),
+                                    dz = __fsub_rn(c.z, me.z);
+                        const float r2t = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                    __fmul_rn(dz, dz));
+                        float tx, ty, tz;
+                        if (kQuad)
+                            cell_term<true>(dx, dy, dz, r2t, c.w, true, s_q[warp][e], s_q2[warp][e].x,
+                                            g, eps2, tx, ty, tz);
+                        else
+                            cell_term<true>(dx, dy, dz, r2t, c.w, false,
+                                            make_float4(0.f, 0.f, 0.f, 0.f), 0.f, g, eps2, tx, ty, tz);
+                        cells.add(tx, ty, tz);
+                    }
+                } else {
+#pragma unroll 2
+                    for (uint32_t e = 0; e < n_cell; ++e) {
+                        const float4 c = s_cm[warp][e];
+                        const float dx = c.x - me.x, dy = c.y - me.y, dz = c.z - me.z;
+                        const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
+                        const float u = inv * inv, inv3 = u * inv;
+                        float ex, ey, ez;
+                        if (kQuad) {
+                            // inv^3 [(M + 5/2 u^2 d.Qd) d - u Qd], u = 1/r^2.
+                            const float4 q = s_q[warp][e];
+                            const float2 q2 = s_q2[warp][e];
+                            const float qx = fmaf(q.x, dx, fmaf(q.z, dy, q.w * dz));
+                            const float qy = fmaf(q.z, dx, fmaf(q.y, dy, q2.x * dz));
+                            const float qz = fmaf(q.w, dx, fmaf(q2.x, dy, q2.y * dz));
+                            const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+                            const float s1 = fmaf(2.5f * u * u, dqd, c.w);
+                            ex = fmaf(s1, dx, -u * qx);
+                            ey = fmaf(s1, dy, -u * qy);
+                            ez = fmaf(s1, dz, -u * qz);
+                        } else {
+                            ex = c.w * dx;
+                            ey = c.w * dy;
+                            ez = c.w * dz;
+                        }
+                        if (kPrec) {
+                            cells.add(inv3 * ex, inv3 * ey, inv3 * ez);
+                        } else {
+                            cells.ax = fmaf(inv3, ex, cells.ax);
+                            cells.ay = fmaf(inv3, ey, cells.ay);
+                            cells.az = fmaf(inv3, ez, cells.az);
+                        }
+                    }
                 }
                 inter += n_cell;
+                cell_inter += n_cell;
             }
             __syncwarp();
             n_cell = 0;
         };
+        // Leaf list: the listed particle ranges are concatenated and staged
+        // 32 particles at a time (a shuffle binary search over the ranges'
+        // prefix sums finds each lane's particle), keeping the walk order.
         auto flush_leaves = [&]() {
-            for (uint32_t e = 0; e < n_leaf; ++e) {
-                const uint2 rg = s_leaf[warp][e];
-                for (uint32_t t = rg.x; t < rg.y; t += 32u) {
-                    const uint32_t j = t + lane;
-                    __syncwarp();
-                    if (j < rg.y) s_tile[warp][lane] = __ldg(&a.pos[j]);
-                    __syncwarp();
-                    const uint32_t cnt = min(32u, rg.y - t);
-                    if (valid) {
+            uint32_t rb = 0, rlen = 0;
+            if (lane < n_leaf) {
+                const uint2 rg = s_leaf[warp][lane];
+                rb = rg.x;
+                rlen = rg.y - rg.x;
+            }
+            uint32_t incl = rlen;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            const uint32_t pre = incl - rlen;
+            const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+            const bool skip_self_free = !kExact && eps2 > 0.f;
+            for (uint32_t t0 = 0; t0 < total; t0 += 32u) {
+                const uint32_t pos = t0 + lane;
+                uint32_t e = 0;
+#pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1) {
+                    const uint32_t cand = e + step;
+                    const uint32_t pc = __shfl_sync(kFullMask, pre, cand & 31u);
+                    if (cand < n_leaf && pc <= pos) e = cand;
+                }
+                const uint32_t eb = __shfl_sync(kFullMask, rb, e);
+                const uint32_t ep = __shfl_sync(kFullMask, pre, e);
+                __syncwarp();
+                if (pos < total) {
+                    const uint32_t j = eb + (pos - ep);
+                    s_tile[warp][lane] = __ldg(&a.pos[j]);
+                    s_jdx[warp][lane] = j;
+                }
+                __syncwarp();
+                const uint32_t cnt = min(32u, total - t0);
+                if (valid) {
+                    if (skip_self_free) {
+                        // eps > 0: the self term is exactly zero, so no test is needed.
+#pragma unroll 4
                         for (uint32_t q = 0; q < cnt; ++q) {
                             const float4 p = s_tile[warp][q];
-                            if (t + q != ip) {
-                                float tx, ty, tz;
-                                particle_term<kExact>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
-                                                      __fsub_rn(p.z, me.z), p.w, g, eps2, tx, ty, tz);
-                                leaves.add(tx, ty, tz);
+                            const float dx = p.x - me.x, dy = p.y - me.y, dz = p.z - me.z;
+                            const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
+                            const float sc = p.w * (inv * inv * inv);
+                            if (kPrec) {
+                                leaves.add(dx * sc, dy * sc, dz * sc);
+                            } else {
+                                leaves.ax = fmaf(dx, sc, leaves.ax);
+                                leaves.ay = fmaf(dy, sc, leaves.ay);
+                                leaves.az = fmaf(dz, sc, leaves.az);
                             }
                         }
-                        inter += cnt - ((ip - t) < cnt ? 1u : 0u);
+                        inter += cnt;
+                    } else {
+                        for (uint32_t q = 0; q < cnt; ++q) {
+                            if (s_jdx[warp][q] == ip) continue;
+                            const float4 p = s_tile[warp][q];
+                            float tx, ty, tz;
+                            particle_term<kExact>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
+                                                  __fsub_rn(p.z, me.z), p.w, kExact ? g : 1.0f, eps2,
+                                                  tx, ty, tz);
+                            leaves.add(tx, ty, tz);
+                            ++inter;
+                        }
                     }
                 }
             }
@@ -507,8 +596,9 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
                         const uint32_t slot = n_cell + __popc(bacc & lt);
                         s_cm[warp][slot] = c;
                         if (kQuad) {
-                            s_q[warp][slot] = __ldg(&a.node_q[nd]);
-                            s_qyz[warp][slot] = __ldg(&a.node_qyz[nd]);
+                            const float4 q = __ldg(&a.node_q[nd]);
+                            s_q[warp][slot] = q;
+                            s_q2[warp][slot] = make_float2(__ldg(&a.node_qyz[nd]), -(q.x + q.y));
                         }
                     }
                     n_cell += __popc(bacc);
@@ -546,12 +636,14 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
         }
         flush_cells();
         flush_leaves();
+        // The self-free fast loop counted the particle's own entry once.
+        if (!kExact && eps2 > 0.f && valid) --inter;
 
         if (valid) {
             const float cl = a.clampv, dt = a.dt;
-            const float sx = kExact ? __fadd_rn(cells.ax, leaves.ax) : cells.ax + leaves.ax;
-            const float sy = kExact ? __fadd_rn(cells.ay, leaves.ay) : cells.ay + leaves.ay;
-            const float sz = kExact ? __fadd_rn(cells.az, leaves.az) : cells.az + leaves.az;
+            const float sx = kExact ? __fadd_rn(cells.ax, leaves.ax) : g * (cells.ax + leaves.ax);
+            const float sy = kExact ? __fadd_rn(cells.ay, leaves.ay) : g * (cells.ay + leaves.ay);
+            const float sz = kExact ? __fadd_rn(cells.az, leaves.az) : g * (cells.az + leaves.az);
             const float ax = fminf(fmaxf(sx, -cl), cl);
             const float ay = fminf(fmaxf(sy, -cl), cl);
             const float az = fminf(fmaxf(sz, -cl), cl);
@@ -576,15 +668,17 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
             }
         }
     }
-    unsigned long long i64 = inter, v64 = visits;
+    unsigned long long i64 = inter, v64 = visits, c64 = cell_inter;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         i64 += __shfl_xor_sync(kFullMask, i64, o);
         v64 += __shfl_xor_sync(kFullMask, v64, o);
+        c64 += __shfl_xor_sync(kFullMask, c64, o);
     }
     if (lane == 0) {
         atomicAdd(&a.stats[0], i64);
         atomicAdd(&a.stats[1], v64);
+        atomicAdd(&a.stats[2], c64);
     }
 }
 

@@ -154,10 +154,11 @@ class Simulation:
         self._check(lib().astro_read_accel(self._h, ptr(out), self.n))
         return out
 
-    def read_stats(self):
-        i, v = c_uint64(), c_uint64()
-        self._check(lib().astro_read_stats(self._h, byref(i), byref(v)))
-        return i.value, v.value
+    def read_stats(self, cells: bool = False):
+        """(interactions, node visits[, cell interactions]) of the last traversal."""
+        i, v, c = c_uint64(), c_uint64(), c_uint64()
+        self._check(lib().astro_read_stats(self._h, byref(i), byref(v), byref(c)))
+        return (i.value, v.value, c.value) if cells else (i.value, v.value)
 
     def direct_accel_f64(self, samples) -> np.ndarray:
         s = np.ascontiguousarray(samples, dtype=np.uint32)

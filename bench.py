@@ -35,7 +35,12 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-updates/s per GB300 step (plain FP32 vs precision+batched) at stated FP64 error"
 UNIT = "particle-updates/s"
-FLOPS_PER_INTERACTION = 20  # the GPU Gems 3 ch. 31 convention for one softened interaction
+# Flops per interaction: 20 for a softened particle-particle or monopole term
+# (the GPU Gems 3 ch. 31 convention); 50 for a cell with its quadrupole term
+# (the monopole's 20 plus Qd (15), d.Qd (5), the radial factor (4) and the
+# two vector updates (6), counting an FMA as 2).
+FLOPS_PER_INTERACTION = 20
+FLOPS_PER_QUAD_CELL = 50
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
 WORKLOADS = {
@@ -61,7 +66,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--form", choices=["plain", "precision"], default="plain")
-    ap.add_argument("--lbits", type=int, default=21)
+    ap.add_argument("--lbits", type=int, default=14)
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--bucket", type=int, default=16)
     ap.add_argument("--warps", type=int, default=0)
@@ -241,8 +246,11 @@ def run_ours(args, world, rank, local):
     sim.synchronize()
     for i, name in enumerate(["bbox+encode", "sort+reorder", "build", "traverse", "integrate"]):
         stages[name] = ev[i].elapsed_time(ev[i + 1])
-    interactions, visits = sim.read_stats()
+    interactions, visits, cell_inter = sim.read_stats(cells=True)
     sizes_, offsets, counts = sim.tree_info()
+    quad = (p.flags & L.FLAG_QUADRUPOLE) != 0
+    flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * cell_inter + \
+        FLOPS_PER_INTERACTION * (interactions - cell_inter)
 
     # Traversal alone, several launches after a flush each, for the roofline.
     trav_ms = []
@@ -263,7 +271,7 @@ def run_ours(args, world, rank, local):
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     peaks, peak_src = measured_peaks()
     fp32_peak = 2 * 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    achieved = interactions * FLOPS_PER_INTERACTION / (trav * 1e-3) / 1e12
+    achieved = flops / (trav * 1e-3) / 1e12
 
     # Error against the FP64 direct sum on sampled particles (current state).
     rng = np.random.default_rng(SEEDS[args.workload])
@@ -309,6 +317,7 @@ def run_ours(args, world, rank, local):
     sim.close()
     return dict(n=n, desc=desc, dt=dt, p=p, value=value, t_ms=t_ms_max, wall=wall,
                 step_ms=step_ms, stages=stages, interactions=interactions, visits=visits,
+                cell_inter=cell_inter, flops=flops,
                 counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
                 fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
                 launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr)
@@ -372,8 +381,11 @@ def run_reference(args):
 
 
 def config_dict(args, desc, n, dt, p):
+    walk = "per-particle" if p.flags & 0x20 else "group"
     return {"workload": f"{args.workload}: {desc}", "n": n, "preset": "PHYSICAL",
-            "form": args.form, "lbits": p.lbits, "theta": p.theta, "eps": p.softening,
+            "form": args.form, "walk": walk, "quadrupole": bool(p.flags & 0x10),
+            "opening": "size/theta + delta" if p.flags & 0x8 else "size/theta",
+            "lbits": p.lbits, "theta": p.theta, "eps": p.softening,
             "dt": dt, "bucket": p.bucket, "G": p.g,
             "l2": "flushed (256 MB write) before every timed step",
             "parallelism": "replicas (one independent system per GPU)"}
@@ -409,7 +421,7 @@ def main():
             "roofline": {"kernel": "traverse_phys_kernel", "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
                          "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
-                         "flops_per_launch": r["interactions"] * FLOPS_PER_INTERACTION,
+                         "flops_per_launch": r["flops"],
                          "launch_ms": r["trav_ms"],
                          "peak_source": f"2 x 128 FP32 lanes x SMs x sm_max_mhz ({r['peak_src']} peaks file)"},
             "cpu_baseline": cpu, "clocks": r["clocks"],
@@ -417,6 +429,7 @@ def main():
                                      "p99": float(np.percentile(r["err"], 99)),
                                      "samples": int(len(r["err"]))},
             "interactions_per_particle": r["interactions"] / r["n"],
+            "cell_interactions_per_particle": r["cell_inter"] / r["n"],
             "node_visits_per_particle": r["visits"] / r["n"],
             "stages_ms": r["stages"], "layer_counts": r["counts"],
         }

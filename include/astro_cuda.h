@@ -235,9 +235,11 @@ int astro_read_tree_info(astro_ctx* ctx, uint32_t* n_layers, uint32_t* layer_siz
 int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t count);
 /* Accelerations (the reference's forceBuffer, float3 with 16-byte stride). */
 int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n);
-/* Traversal statistics of the last traversal: total interactions (monopole +
- * particle-particle) and nodes visited, summed over particles. */
-int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits);
+/* Traversal statistics of the last traversal, summed over particles: all
+ * interactions (cell + particle-particle), nodes tested, and the cell
+ * (accepted node) interactions among them. */
+int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits,
+                     uint64_t* cell_interactions);
 
 /* FP64 direct-sum accelerations (G, eps as the context's PHYSICAL params) of
  * the sampled particles against all particles of their own system, computed
