@@ -71,11 +71,25 @@ def parse():
     ap.add_argument("--bucket", type=int, default=16)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--persistent", action="store_true")
+    ap.add_argument("--walk", choices=["group", "particle"], default="group")
+    ap.add_argument("--monopole", action="store_true",
+                    help="the reference's monopole-only cells and size/theta opening test")
     ap.add_argument("--error-samples", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
+
+
+def walk_flags(args, L, flags):
+    """Traversal flags: the preset's defaults adjusted by --walk/--monopole."""
+    if args.walk == "particle":
+        flags |= L.FLAG_PER_PARTICLE
+    if args.monopole:
+        flags &= ~(L.FLAG_QUADRUPOLE | L.FLAG_OPEN_DELTA)
+    if args.persistent:
+        flags |= L.FLAG_PERSISTENT
+    return flags
 
 
 def make_inputs(ic, workload):
@@ -187,11 +201,10 @@ def run_ours(args, world, rank, local):
     desc, _, _, over, dt = WORKLOADS[args.workload]
     pm, vr, sizes = make_inputs(ic, args.workload)
     n = len(pm)
-    flags = L.FLAG_PERSISTENT if args.persistent else 0
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
-                          bucket=args.bucket, block_warps=args.warps, flags=flags, form=form,
-                          **over)
+                          bucket=args.bucket, block_warps=args.warps, form=form, **over)
+    p = p.replace(flags=walk_flags(args, L, p.flags))
     nsys = len(sizes) if sizes else 1
     sim = ag.Simulation(p, max_n=n, max_systems=nsys)
     upload = (lambda: sim.upload_systems(pm, vr, sizes)) if sizes else (lambda: sim.upload(pm, vr))
@@ -358,6 +371,7 @@ def run_reference(args):
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
                           bucket=args.bucket, form=form, **over)
+    p = p.replace(flags=walk_flags(args, L, p.flags))
     cores = orc.set_threads(0)
     pm_c, vr_c = pm.copy(), vr.copy()
     for _ in range(args.warmup):
