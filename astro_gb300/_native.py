@@ -67,6 +67,8 @@ SIGNATURES = {
     "astro_radix_sort_temp_bytes": (c_int, [c_uint32, c_uint32, POINTER(c_size_t)]),
     "astro_radix_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p,
                                  c_uint32, c_void_p, c_size_t, c_void_p]),
+    "astro_radix_sort_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32,
+                                         c_void_p, c_uint32, c_void_p]),
     "astro_generate_ic": (c_int, [c_uint32, c_uint64, c_uint32, c_uint32, c_double, c_double,
                                   c_void_p, c_void_p, c_void_p]),
     "astro_generate_system_sizes": (c_int, [c_uint64, c_uint32, c_uint32, c_uint32, c_double,

@@ -272,6 +272,25 @@ int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
                      void* stream);
 
 /* ---------------------------------------------------------------------------
+ * The same sort for callers that cannot allocate device memory (no
+ * counterpart in the reference). Hosts whose device memory belongs to another
+ * allocator, frame loops with a fixed preallocated budget, and embedders that
+ * forbid allocation after start-up cannot supply or create a temporary
+ * buffer; this entry point uses a static device array of the library instead
+ * and allocates nothing. It sorts at most ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH
+ * pairs (larger estimated_length returns ASTRO_ERR_CAPACITY); every GPU that
+ * loads the library holds the array (about 14 MiB) until exit. All calls on a
+ * device share the array: calls that overlap on the GPU race, so serialise
+ * them. The first call on a device resolves the array's address there; make
+ * it before any stream capture begins.
+ * ------------------------------------------------------------------------- */
+#define ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH 1048576u
+int astro_radix_sort_noalloc(const uint64_t* d_input, const uint32_t* d_input_indices,
+                             uint64_t* d_output, uint32_t* d_output_indices,
+                             uint32_t estimated_length, const uint32_t* d_actual_count,
+                             uint32_t key_bits, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Seeded initial conditions (host side, FP64 then cast). Counter-based
  * Philox4x32-10 streams keyed by (seed, system, particle), so any host
  * produces identical sets. Replaces Renderer.makeSpheres (Renderer.swift:441-493).
