@@ -287,11 +287,7 @@ __global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
         st_relaxed_u32(word, (tile == 0 ? kLbInclusive : kLbAggregate) | run);
         uint32_t prefix = 0;
         if (tile > 0) {
-            for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
-                const uint32_t v = lookback_wait(a.lookback + (size_t)j * 32 + tid, a.err);
-                prefix += v & kLbCountMask;
-                if ((v & kLbInclusive) != 0) break;
-            }
+            prefix = lookback_window(a.lookback, tile, tid, a.err, 32);
             st_relaxed_u32(word, kLbInclusive | (prefix + run));
         }
         s_prefix[tid] = prefix;

@@ -109,4 +109,37 @@ __device__ __forceinline__ uint32_t lookback_wait(const uint32_t* word, uint32_t
     return v;
 }
 
+// Decoupled look-back for the status word of column `col` (`stride` words
+// per tile) of tiles before `tile`: reads kLbWindow predecessors per
+// round so that one memory latency covers several tiles, adds their counts
+// back to the first inclusive one, and re-polls (bounded) a word that is not
+// published yet. Returns the exclusive prefix of tile `tile`.
+constexpr int kLbWindow = 8;
+__device__ __forceinline__ uint32_t lookback_window(const uint32_t* words, uint32_t tile,
+                                                    uint32_t col, uint32_t* err,
+                                                    uint32_t stride = 256) {
+    uint32_t prefix = 0;
+    int64_t j = (int64_t)tile - 1;
+    while (j >= 0) {
+        uint32_t v[kLbWindow];
+#pragma unroll
+        for (int k = 0; k < kLbWindow; ++k)
+            v[k] = (j - k >= 0) ? ld_relaxed_u32(words + (size_t)(j - k) * stride + col) : kLbInclusive;
+        int k = 0;
+        for (; k < kLbWindow; ++k) {
+            if ((v[k] >> 30) == 0) break;  // not published yet: wait on it below
+            prefix += v[k] & kLbCountMask;
+            if ((v[k] & kLbInclusive) != 0) return prefix;
+        }
+        j -= k;
+        if (k < kLbWindow) {
+            const uint32_t w = lookback_wait(words + (size_t)j * stride + col, err);
+            prefix += w & kLbCountMask;
+            if ((w & kLbInclusive) != 0) return prefix;
+            --j;
+        }
+    }
+    return prefix;
+}
+
 }  // namespace astro

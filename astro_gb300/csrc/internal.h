@@ -44,6 +44,9 @@ struct SortPlan {
     size_t keys_tmp, vals_tmp, excl, zero_begin, hist, counters, lookback, zero_end, total;
     uint32_t passes, ntiles, tile;
 };
+// Pairs per tile assumed when sizing the look-back words (the smallest tile
+// of any pass variant, 256 threads x 8 pairs).
+constexpr uint32_t kSortPlanTile = 2048;
 SortPlan sort_plan(uint32_t max_len, uint32_t key_bits);
 cudaError_t sort_init();
 // Stable sort of n_est (key, value) pairs (count read from d_count when not

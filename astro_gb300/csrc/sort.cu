@@ -15,6 +15,8 @@
 //      as contiguous stores.
 // A stable LSD sort yields the one stable permutation, so the result equals
 // the reference's bit by bit, including the order of equal keys.
+#include <cstdlib>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -23,11 +25,9 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
-constexpr int kTile = kThreads * kItems;  // 4096 pairs per tile
 constexpr int kRadix = 256;
 constexpr int kMaxPasses = 8;
-constexpr int kHistBlocksPerSm = 4;
+constexpr int kHistBlocksPerSm = 8;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -68,35 +68,58 @@ __device__ __forceinline__ uint32_t peer_mask(uint32_t digit, uint32_t bits, uin
     return peers;
 }
 
+// All digit histograms in one read of the keys. Each warp counts into its own
+// shared-memory copy with atomics; a warp whose 32 keys share a digit (the
+// usual case for the high digits of Morton keys of a Morton-ordered state)
+// adds 32 with a single atomic.
 __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(
     const uint64_t* __restrict__ keys, const uint32_t* __restrict__ d_count, uint32_t n_est,
     uint32_t key_bits, uint32_t passes, uint32_t* __restrict__ hist, uint32_t* __restrict__ excl,
     uint32_t* __restrict__ done) {
-    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    extern __shared__ uint32_t s_hist[];  // [kWarps][passes][kRadix]
     __shared__ uint32_t s_warp[kWarps];
     __shared__ bool s_last;
-    const uint32_t tid = threadIdx.x;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t n = d_count ? min(*d_count, n_est) : n_est;
-    for (uint32_t i = tid; i < passes * kRadix; i += kThreads) s_hist[i] = 0;
+    const uint32_t per_warp = passes * kRadix;
+    for (uint32_t i = tid; i < kWarps * per_warp; i += kThreads) s_hist[i] = 0;
     __syncthreads();
-    const uint32_t lt = lanemask_lt();
-    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t base = (uint64_t)blockIdx.x * kThreads; base < n; base += stride) {
-        const uint64_t i = base + tid;
-        const bool valid = i < n;
-        const uint64_t key = valid ? __ldcs(keys + i) : 0ull;
-        const uint32_t vmask = __ballot_sync(kFullMask, valid);
-        for (uint32_t p = 0; p < passes; ++p) {
-            const uint32_t shift = 8u * p;
-            const uint32_t bits = min(8u, key_bits - shift);
-            const uint32_t digit = (uint32_t)(key >> shift) & ((1u << bits) - 1u);
-            const uint32_t peers = peer_mask(digit, bits, vmask);
-            if (valid && (peers & lt) == 0) atomicAdd(&s_hist[p * kRadix + digit], __popc(peers));
+    uint32_t* my_hist = s_hist + warp * per_warp;
+    // Each thread takes kHistKeys keys per round (independent loads in flight).
+    constexpr int kHistKeys = 4;
+    const uint64_t stride = (uint64_t)gridDim.x * kThreads * kHistKeys;
+    for (uint64_t base = (uint64_t)blockIdx.x * kThreads * kHistKeys; base < n; base += stride) {
+        uint64_t key[kHistKeys];
+        bool valid[kHistKeys];
+#pragma unroll
+        for (int k = 0; k < kHistKeys; ++k) {
+            const uint64_t i = base + (uint64_t)k * kThreads + tid;
+            valid[k] = i < n;
+            key[k] = valid[k] ? __ldcs(keys + i) : 0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < kHistKeys; ++k) {
+            const bool full = __all_sync(kFullMask, valid[k]);
+            for (uint32_t p = 0; p < passes; ++p) {
+                const uint32_t shift = 8u * p;
+                const uint32_t bits = min(8u, key_bits - shift);
+                const uint32_t digit = (uint32_t)(key[k] >> shift) & ((1u << bits) - 1u);
+                const bool same =
+                    full && __all_sync(kFullMask, digit == __shfl_sync(kFullMask, digit, 0));
+                if (same) {
+                    if (lane == 0) atomicAdd(&my_hist[p * kRadix + digit], 32u);
+                } else if (valid[k]) {
+                    atomicAdd(&my_hist[p * kRadix + digit], 1u);
+                }
+            }
         }
     }
     __syncthreads();
-    for (uint32_t i = tid; i < passes * kRadix; i += kThreads)
-        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+    for (uint32_t i = tid; i < per_warp; i += kThreads) {
+        uint32_t c = 0;
+        for (int w = 0; w < kWarps; ++w) c += s_hist[w * per_warp + i];
+        if (c) atomicAdd(&hist[i], c);
+    }
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
@@ -109,7 +132,9 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(
     }
 }
 
+template <int kItems>
 struct PassSmem {
+    static constexpr int kTile = kThreads * kItems;
     union {
         uint32_t warp_hist[kWarps][kRadix];  // ranking: per-warp digit counters
         struct {
@@ -123,14 +148,20 @@ struct PassSmem {
     uint32_t tile_id;
 };
 
-__global__ __launch_bounds__(kThreads, 2) void sort_pass_kernel(
+// One onesweep pass. kItems pairs per thread; kMatch ranks with
+// __match_any_sync and one shared atomic per distinct digit, otherwise with
+// per-bit ballots and per-warp counters.
+template <int kItems, int kMinBlocks, bool kMatch>
+__global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
     const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
     uint32_t digit_bits, uint32_t* __restrict__ err) {
+    using Smem = PassSmem<kItems>;
+    constexpr int kTile = Smem::kTile;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PassSmem& sm = *reinterpret_cast<PassSmem*>(smem_raw);
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t n = d_count ? min(*d_count, n_est) : n_est;
     if (tid == 0) sm.tile_id = atomicAdd(tile_counter, 1u);
@@ -160,14 +191,23 @@ __global__ __launch_bounds__(kThreads, 2) void sort_pass_kernel(
         const uint64_t i = warp_base + 32ull * k + lane;
         const bool valid = i < n;
         const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
-        const uint32_t peers = peer_mask(digit, digit_bits, __ballot_sync(kFullMask, valid));
-        const uint32_t lower = __popc(peers & lt), cnt = __popc(peers);
-        uint32_t old = 0;
-        if (valid) old = sm.u.warp_hist[warp][digit];
-        __syncwarp();
-        if (valid && lower + 1 == cnt) sm.u.warp_hist[warp][digit] = old + cnt;
-        __syncwarp();
-        pos[k] = old + lower;
+        if (kMatch) {
+            const uint32_t peers = __match_any_sync(kFullMask, valid ? digit : (256u + lane));
+            const uint32_t leader = 31u - __clz(peers);
+            uint32_t old = 0;
+            if (valid && lane == leader) old = atomicAdd(&sm.u.warp_hist[warp][digit], __popc(peers));
+            old = __shfl_sync(kFullMask, old, leader);
+            pos[k] = old + __popc(peers & lt);
+        } else {
+            const uint32_t peers = peer_mask(digit, digit_bits, __ballot_sync(kFullMask, valid));
+            const uint32_t lower = __popc(peers & lt), cnt = __popc(peers);
+            uint32_t old = 0;
+            if (valid) old = sm.u.warp_hist[warp][digit];
+            __syncwarp();
+            if (valid && lower + 1 == cnt) sm.u.warp_hist[warp][digit] = old + cnt;
+            __syncwarp();
+            pos[k] = old + lower;
+        }
     }
     __syncthreads();
 
@@ -185,11 +225,7 @@ __global__ __launch_bounds__(kThreads, 2) void sort_pass_kernel(
     sm.tile_start[tid] = tile_start;
     uint32_t prefix = 0;
     if (tile > 0) {
-        for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
-            const uint32_t v = lookback_wait(lookback + (size_t)j * kRadix + tid, err);
-            prefix += v & kLbCountMask;
-            if ((v & kLbInclusive) != 0) break;
-        }
+        prefix = lookback_window(lookback, tile, tid, err);
         st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
     }
     sm.global_base[tid] = excl[tid] + prefix;
@@ -220,6 +256,27 @@ __global__ __launch_bounds__(kThreads, 2) void sort_pass_kernel(
     }
 }
 
+// Pass-kernel variants (items per thread, blocks per SM, ranking).
+struct PassVariant {
+    int items;
+    void (*kernel)(const uint64_t*, const uint32_t*, uint64_t*, uint32_t*, const uint32_t*, uint32_t,
+                   const uint32_t*, uint32_t*, uint32_t*, uint32_t, uint32_t, uint32_t*);
+    size_t smem;
+};
+const PassVariant kVariants[] = {
+    {16, sort_pass_kernel<16, 2, false>, sizeof(PassSmem<16>)},
+    {16, sort_pass_kernel<16, 2, true>, sizeof(PassSmem<16>)},
+    {12, sort_pass_kernel<12, 3, true>, sizeof(PassSmem<12>)},
+    {8, sort_pass_kernel<8, 4, true>, sizeof(PassSmem<8>)},
+    {20, sort_pass_kernel<20, 2, true>, sizeof(PassSmem<20>)},
+    {12, sort_pass_kernel<12, 3, false>, sizeof(PassSmem<12>)},
+    {8, sort_pass_kernel<8, 4, false>, sizeof(PassSmem<8>)},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+constexpr int kMinItems = 8;  // sizes the look-back words for every variant
+static_assert(kThreads * kMinItems == (int)kSortPlanTile, "look-back sizing");
+int g_variant = 5;
+
 int g_num_sms = 0;
 
 int num_sms() {
@@ -239,8 +296,19 @@ int num_sms() {
 cudaError_t sort_init() {
     static bool done = false;
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(sort_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(PassSmem));
+    cudaError_t e = cudaSuccess;
+    for (int v = 0; v < kNumVariants; ++v) {
+        e = cudaFuncSetAttribute(kVariants[v].kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kVariants[v].smem);
+        if (e != cudaSuccess) return e;
+    }
+    // Tuning knob for benchmarks: ASTRO_SORT_VARIANT selects a pass variant.
+    if (const char* env = getenv("ASTRO_SORT_VARIANT")) {
+        const int v = atoi(env);
+        if (v >= 0 && v < kNumVariants) g_variant = v;
+    }
+    e = cudaFuncSetAttribute(sort_histogram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kWarps * kMaxPasses * kRadix * sizeof(uint32_t)));
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -248,8 +316,8 @@ cudaError_t sort_init() {
 SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
     SortPlan p{};
     p.passes = key_bits == 0 ? 1u : (key_bits + 7u) / 8u;
-    p.tile = kTile;
-    p.ntiles = (uint32_t)(((uint64_t)max_len + kTile - 1) / kTile);
+    p.tile = kSortPlanTile;
+    p.ntiles = (uint32_t)(((uint64_t)max_len + p.tile - 1) / p.tile);
     size_t off = 0;
     p.keys_tmp = off;
     off = align_up(off + 8ull * max_len, 256);
@@ -276,9 +344,11 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
     if (n_est == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(n_est, key_bits);
     if (temp_bytes < plan.total || key_bits > 64) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(PassSmem);
     cudaError_t e0 = sort_init();
     if (e0 != cudaSuccess) return e0;
+    const PassVariant& pv = kVariants[g_variant];
+    const uint32_t tile = (uint32_t)(kThreads * pv.items);
+    const uint32_t ntiles = (uint32_t)(((uint64_t)n_est + tile - 1) / tile);
     char* base = static_cast<char*>(temp);
     uint64_t* keys_tmp = reinterpret_cast<uint64_t*>(base + plan.keys_tmp);
     uint32_t* vals_tmp = reinterpret_cast<uint32_t*>(base + plan.vals_tmp);
@@ -290,9 +360,10 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
     cudaError_t e = cudaMemsetAsync(base + plan.zero_begin, 0, plan.zero_end - plan.zero_begin, st);
     if (e != cudaSuccess) return e;
     const uint32_t hist_blocks = (uint32_t)std::min<uint64_t>(
-        ((uint64_t)n_est + kThreads - 1) / kThreads, (uint64_t)num_sms() * kHistBlocksPerSm);
-    sort_histogram_kernel<<<hist_blocks, kThreads, 0, st>>>(keys_in, d_count, n_est, key_bits,
-                                                            plan.passes, hist, excl, counters + 8);
+        ((uint64_t)n_est + 4 * kThreads - 1) / (4 * kThreads), (uint64_t)num_sms() * kHistBlocksPerSm);
+    const size_t hist_smem = (size_t)kWarps * plan.passes * kRadix * sizeof(uint32_t);
+    sort_histogram_kernel<<<hist_blocks, kThreads, hist_smem, st>>>(keys_in, d_count, n_est, key_bits,
+                                                                    plan.passes, hist, excl, counters + 8);
     const uint64_t* kin = keys_in;
     const uint32_t* vin = vals_in;
     for (uint32_t p = 0; p < plan.passes; ++p) {
@@ -301,7 +372,7 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
         uint32_t* vout = to_out ? vals_out : vals_tmp;
         const uint32_t shift = 8u * p;
         const uint32_t bits = key_bits == 0 ? 0u : std::min(8u, key_bits - shift);
-        sort_pass_kernel<<<plan.ntiles, kThreads, smem, st>>>(
+        pv.kernel<<<ntiles, kThreads, pv.smem, st>>>(
             kin, vin, kout, vout, d_count, n_est, excl + p * kRadix,
             lookback + (size_t)p * plan.ntiles * kRadix, counters + p, shift, bits, err);
         kin = kout;

@@ -7,7 +7,7 @@
 // embedding hosts that forbid cudaMalloc after start-up. For them this file
 // keeps the sort's scratch in a file-scope device array, sized for at most
 // kNoAllocMaxLength pairs. Every GPU that loads the library holds the array
-// (about 14 MiB) until the process exits.
+// (about 16 MiB) until the process exits.
 //
 // The array is shared by every call on a device and keeps what the last call
 // left in it; the sort clears the parts that must start at zero (histograms,
@@ -29,8 +29,8 @@ constexpr uint32_t kNoAllocMaxLength = ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH;
 
 // Bytes of sort_plan(kNoAllocMaxLength, 64): ping-pong keys (8 B) and values
 // (4 B), 8 passes of 256-bin offsets and histograms, the counters and 8
-// passes of 256 look-back words per 4096-pair tile, each region 256-aligned.
-constexpr size_t kTiles = (kNoAllocMaxLength + 4095) / 4096;
+// passes of 256 look-back words per tile, each region 256-aligned.
+constexpr size_t kTiles = (kNoAllocMaxLength + astro::kSortPlanTile - 1) / astro::kSortPlanTile;
 constexpr size_t kNoAllocBytes = 8ull * kNoAllocMaxLength + 4ull * kNoAllocMaxLength +
                                  4ull * 8 * 256 + 4ull * 8 * 256 + 256 + 4ull * 8 * kTiles * 256;
 

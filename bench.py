@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--one-at-a-time", action="store_true",
+                    help="batched workload: also time the systems stepped one at a time")
     return ap.parse_args()
 
 
@@ -325,6 +327,39 @@ def run_ours(args, world, rank, local):
                "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 64 * n,
                "ms_per_step": te * 1e3 / args.steps}
 
+    # Batched workload: the same systems launched one at a time (one context
+    # and one step graph per system, stepped in sequence).
+    one_at_a_time = None
+    if sizes and args.one_at_a_time:
+        sims, off = [], 0
+        p_plain = p.replace(form=L.FORM_PLAIN)
+        for sz in sizes:
+            s1 = ag.Simulation(p_plain, max_n=sz)
+            s1.upload(pm[off:off + sz], vr[off:off + sz])
+            off += sz
+            s1.draw(dt, 2)
+            sims.append(s1)
+        for s1 in sims:
+            s1.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        k1 = max(1, args.steps // 4)
+        e0.record()
+        for _ in range(k1):
+            for s1 in sims:
+                s1.draw(dt, 1)
+        for s1 in sims:
+            s1.synchronize()
+        e1.record()
+        torch.cuda.synchronize()
+        t1 = e0.elapsed_time(e1)
+        one_at_a_time = {"value": n * k1 / (t1 * 1e-3), "unit": UNIT, "steps": k1,
+                         "ms_per_step": t1 / k1,
+                         "how": "plain FP32, one context and step graph per system, "
+                                "stepped in sequence"}
+        for s1 in sims:
+            s1.close()
+
     passes = (3 * args.lbits + (int(np.ceil(np.log2(nsys))) if nsys > 1 else 0) + 7) // 8
     launches_per_step = 7 + passes + (args.lbits + 1)
     sim.close()
@@ -333,7 +368,8 @@ def run_ours(args, world, rank, local):
                 cell_inter=cell_inter, flops=flops,
                 counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
                 fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
-                launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr)
+                launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr,
+                one_at_a_time=one_at_a_time)
 
 
 # ----------------------------------------------------------- CPU side --
@@ -446,6 +482,7 @@ def main():
             "cell_interactions_per_particle": r["cell_inter"] / r["n"],
             "node_visits_per_particle": r["visits"] / r["n"],
             "stages_ms": r["stages"], "layer_counts": r["counts"],
+            "systems_one_at_a_time": r["one_at_a_time"],
         }
         print(json.dumps(line))
     if world > 1:

@@ -279,7 +279,7 @@ int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
  * buffer; this entry point uses a static device array of the library instead
  * and allocates nothing. It sorts at most ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH
  * pairs (larger estimated_length returns ASTRO_ERR_CAPACITY); every GPU that
- * loads the library holds the array (about 14 MiB) until exit. All calls on a
+ * loads the library holds the array (about 16 MiB) until exit. All calls on a
  * device share the array: calls that overlap on the GPU race, so serialise
  * them. The first call on a device resolves the array's address there; make
  * it before any stream capture begins.
