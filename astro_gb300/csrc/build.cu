@@ -430,11 +430,15 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
 }
 
 // aggregateNodes (Octree.metal:120-202), one thread per node of layer l.
-// Children are the contiguous run of layer l-1 nodes sharing code >> 3.
+// Children are the contiguous run of layer l-1 nodes sharing code >> 3 (at
+// most 8). Each thread first loads all its children's records together
+// (one memory latency instead of one per child), then sums them in child
+// order with the same roundings as a sequential loop.
 // kMode 0 sums child centre of mass times child mass (the reference's
 // formula); kModes 1 and 2 add the children's raw sums.
 template <int kMode>
-__global__ void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off, uint32_t off_below) {
+__global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off,
+                                                                 uint32_t off_below) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t u = a.layer_count[l];
     if (j >= u) return;
@@ -443,41 +447,64 @@ __global__ void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off, u
     const uint32_t ce = (j + 1 < u) ? a.node_cbeg[node + 1] : off_below + a.layer_count[l - 1];
     const uint32_t pb = a.pbeg[node];
     const uint32_t pe = (j + 1 < u) ? a.pbeg[node + 1] : a.n;
-    a.node_key[node] = a.sorted_keys[pb] >> (3u * l);
+    if (ce - cb > 8u) atomicOr(a.err, kErrBadLayer);
+    const uint32_t nch = min(ce - cb, 8u);
+    const uint64_t key = a.sorted_keys[pb];
+    a.node_key[node] = key >> (3u * l);
     float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ccm[8];  // children's centres of mass (modes 0 and quadrupoles)
+    const bool need_ccm = kMode == 0 || (kMode != 0 && a.want_quad);
+    if (need_ccm) {
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            ccm[k] = k < nch ? a.node_cm[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     if (kMode == 0) {
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
-        for (uint32_t c = cb; c < ce; ++c) {
-            const float4 q = a.node_cm[c];
-            m = __fadd_rn(m, q.w);
-            sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
-            sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
-            sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            if (k < nch) {
+                const float4 q = ccm[k];
+                m = __fadd_rn(m, q.w);
+                sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
+                sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
+                sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
+            }
         }
         if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
         else cm.w = m;
     } else if (kMode == 1) {
         const float4* sum = reinterpret_cast<const float4*>(a.node_sum);
+        float4 cs[8];
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? sum[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
-        for (uint32_t c = cb; c < ce; ++c) {
-            const float4 q = sum[c];
-            sx = __fadd_rn(sx, q.x);
-            sy = __fadd_rn(sy, q.y);
-            sz = __fadd_rn(sz, q.z);
-            m = __fadd_rn(m, q.w);
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            if (k < nch) {
+                sx = __fadd_rn(sx, cs[k].x);
+                sy = __fadd_rn(sy, cs[k].y);
+                sz = __fadd_rn(sz, cs[k].z);
+                m = __fadd_rn(m, cs[k].w);
+            }
         }
         reinterpret_cast<float4*>(a.node_sum)[node] = make_float4(sx, sy, sz, m);
         if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
         else cm.w = m;
     } else {
         const double4* sum = reinterpret_cast<const double4*>(a.node_sum);
+        double4 cs[8];
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? sum[cb + k] : make_double4(0.0, 0.0, 0.0, 0.0);
         double m = 0, sx = 0, sy = 0, sz = 0;
-        for (uint32_t c = cb; c < ce; ++c) {
-            const double4 q = sum[c];
-            sx = __dadd_rn(sx, q.x);
-            sy = __dadd_rn(sy, q.y);
-            sz = __dadd_rn(sz, q.z);
-            m = __dadd_rn(m, q.w);
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            if (k < nch) {
+                sx = __dadd_rn(sx, cs[k].x);
+                sy = __dadd_rn(sy, cs[k].y);
+                sz = __dadd_rn(sz, cs[k].z);
+                m = __dadd_rn(m, cs[k].w);
+            }
         }
         reinterpret_cast<double4*>(a.node_sum)[node] = make_double4(sx, sy, sz, m);
         if (m > 0.0)
@@ -489,39 +516,55 @@ __global__ void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off, u
     a.node_rng[node] = make_uint4(cb, ce, pb, pe);
     if (kMode != 0) {
         if (a.want_quad) {
+            float4 qc[8];
+            float qyz[8];
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                qc[k] = k < nch ? a.node_q[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+                qyz[k] = k < nch ? a.node_qyz[cb + k] : 0.f;
+            }
             float q[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-            for (uint32_t c = cb; c < ce; ++c) {
-                const float4 cc = a.node_cm[c];
-                quad_add(q, cc.w, __fsub_rn(cc.x, cm.x), __fsub_rn(cc.y, cm.y), __fsub_rn(cc.z, cm.z));
-                const float4 qc = a.node_q[c];
-                q[0] = __fadd_rn(q[0], qc.x);
-                q[1] = __fadd_rn(q[1], qc.y);
-                q[2] = __fadd_rn(q[2], qc.z);
-                q[3] = __fadd_rn(q[3], qc.w);
-                q[4] = __fadd_rn(q[4], a.node_qyz[c]);
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                if (k < nch) {
+                    const float4 cc = ccm[k];
+                    quad_add(q, cc.w, __fsub_rn(cc.x, cm.x), __fsub_rn(cc.y, cm.y), __fsub_rn(cc.z, cm.z));
+                    q[0] = __fadd_rn(q[0], qc[k].x);
+                    q[1] = __fadd_rn(q[1], qc[k].y);
+                    q[2] = __fadd_rn(q[2], qc[k].z);
+                    q[3] = __fadd_rn(q[3], qc[k].w);
+                    q[4] = __fadd_rn(q[4], qyz[k]);
+                }
             }
             a.node_q[node] = make_float4(q[0], q[1], q[2], q[3]);
             a.node_qyz[node] = q[4];
         }
-        if (a.want_delta) a.node_crit2[node] = node_crit2(a, a.sorted_keys[pb], l, cm);
+        if (a.want_delta) a.node_crit2[node] = node_crit2(a, key, l, cm);
         // Groups: a node over the group size packs runs of consecutive
         // small children (greedy, in child order); a small top-layer node is
         // a group by itself.
         if (pe - pb > kGroupSize) {
+            uint2 cr[8];
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                const uint4* rng = a.node_rng + cb + k;
+                cr[k] = k < nch ? make_uint2(__ldg(&rng->z), __ldg(&rng->w)) : make_uint2(0u, 0u);
+            }
             uint32_t gb = 0, ge = 0;
-            for (uint32_t c = cb; c < ce; ++c) {
-                const uint4 rc = a.node_rng[c];
-                const uint32_t cc = rc.w - rc.z;
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                if (k >= nch) break;
+                const uint32_t cc = cr[k].y - cr[k].x;
                 if (cc <= kGroupSize) {
                     if (ge == gb) {
-                        gb = rc.z;
-                        ge = rc.w;
+                        gb = cr[k].x;
+                        ge = cr[k].y;
                     } else if ((ge - gb) + cc <= kGroupSize) {
-                        ge = rc.w;
+                        ge = cr[k].y;
                     } else {
                         emit_group(a, gb, ge);
-                        gb = rc.z;
-                        ge = rc.w;
+                        gb = cr[k].x;
+                        ge = cr[k].y;
                     }
                 } else if (ge != gb) {
                     emit_group(a, gb, ge);

@@ -46,6 +46,7 @@ struct AggArgs {
     uint32_t want_quad;
     uint32_t want_delta;
     float theta;
+    uint32_t* err;         // device error word (kErrBadLayer: a node with > 8 children)
 };
 
 constexpr uint32_t kGroupSize = 32;  // particles per group walk (one warp)

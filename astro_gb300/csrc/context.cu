@@ -277,6 +277,7 @@ int stage_build(astro_ctx* ctx) {
     a.want_quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.want_delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
     a.theta = ctx->p.theta;
+    a.err = ctx->err;
     CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
     const int mode = !is_phys(ctx) ? 0 : (is_prec(ctx) ? 2 : 1);
     CK(astro::launch_aggregate(mode, a, ctx->layers, st));

@@ -188,6 +188,32 @@ struct Accum {
         add1(ay, cy, ty);
         add1(az, cz, tz);
     }
+
+    // Blocked form (group walk, exact): with Kahan, terms are added plainly
+    // within blocks of 32 consecutive list positions and each block's
+    // partial is Kahan-added by step(); every position steps, including a
+    // particle's own skipped one. Without Kahan, push() is add().
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    uint32_t k = 0;
+    __device__ __forceinline__ void push(float tx, float ty, float tz) {
+        if (kKahan) {
+            bx = kExact ? __fadd_rn(bx, tx) : bx + tx;
+            by = kExact ? __fadd_rn(by, ty) : by + ty;
+            bz = kExact ? __fadd_rn(bz, tz) : bz + tz;
+        } else {
+            add(tx, ty, tz);
+        }
+    }
+    __device__ __forceinline__ void close() {
+        add(bx, by, bz);
+        bx = by = bz = 0.f;
+    }
+    __device__ __forceinline__ void step() {
+        if (kKahan && (++k & 31u) == 0u) close();
+    }
+    __device__ __forceinline__ void finish() {
+        if (kKahan && (k & 31u) != 0u) close();
+    }
 };
 
 template <bool kExact, bool kPrec, bool kBatched, bool kPersistent, int kWarps>
@@ -376,9 +402,19 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
 // sum, leaf particles (32 at a time through shared memory) into another.
 constexpr int kCellCap = 64;
 constexpr int kLeafCap = 32;
+// Resident warps per SM the group walk's register allocation is sized for
+// (0: the compiler's choice).
+#ifndef ASTRO_GROUP_WARPS_PER_SM
+#define ASTRO_GROUP_WARPS_PER_SM 0
+#endif
+#if ASTRO_GROUP_WARPS_PER_SM > 0
+#define ASTRO_GROUP_BOUNDS(w) __launch_bounds__((w) * 32, ASTRO_GROUP_WARPS_PER_SM / (w))
+#else
+#define ASTRO_GROUP_BOUNDS(w) __launch_bounds__((w) * 32)
+#endif
 
 template <bool kExact, bool kPrec, bool kQuad, int kWarps>
-__global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArgs a) {
+__global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a) {
     __shared__ float4 s_cm[kWarps][kCellCap];
     __shared__ float4 s_q[kWarps][kQuad ? kCellCap : 1];   // Qxx, Qyy, Qxy, Qxz
     __shared__ float2 s_q2[kWarps][kQuad ? kCellCap : 1];  // Qyz, Qzz
@@ -401,8 +437,15 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
         if (gi >= ngroups) break;
         const uint2 gr = a.groups[gi];
         const uint32_t gcount = gr.y - gr.x;
-        const bool valid = lane < gcount;
-        const uint32_t ip = gr.x + lane;
+        // A group of at most 16 particles runs as reps = 32 / gcount copies
+        // (lane = rep * gcount + particle), each copy summing every reps-th
+        // listed source; the copies' partial sums are added at the end. The
+        // exact form keeps one copy, for the CPU restatement's order.
+        const uint32_t reps = kExact ? 1u : max(1u, 32u / gcount);
+        const uint32_t rep = lane / gcount;
+        const bool valid = rep < reps;   // the lane holds a copy of a particle
+        const bool owner = rep == 0;     // the copy that writes the particle
+        const uint32_t ip = gr.x + (lane - rep * gcount);
         const float4 me = valid ? a.pos[ip] : make_float4(0.f, 0.f, 0.f, 0.f);
         const uint32_t sys = a.nsys > 1 ? (uint32_t)(a.sorted_keys[gr.x] >> (3u * a.lbits)) : 0u;
         const float* crit_layer = a.sys[sys].crit2;
@@ -442,11 +485,18 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
                         else
                             cell_term<true>(dx, dy, dz, r2t, c.w, false,
                                             make_float4(0.f, 0.f, 0.f, 0.f), 0.f, g, eps2, tx, ty, tz);
-                        cells.add(tx, ty, tz);
+                        cells.push(tx, ty, tz);
+                        cells.step();
                     }
                 } else {
+                    // Precision form: this flush's terms go into a partial
+                    // that is Kahan-added once.
+                    float px = 0.f, py = 0.f, pz = 0.f;
+                    float& rx = kPrec ? px : cells.ax;
+                    float& ry = kPrec ? py : cells.ay;
+                    float& rz = kPrec ? pz : cells.az;
 #pragma unroll 2
-                    for (uint32_t e = 0; e < n_cell; ++e) {
+                    for (uint32_t e = rep; e < n_cell; e += reps) {
                         const float4 c = s_cm[warp][e];
                         const float dx = c.x - me.x, dy = c.y - me.y, dz = c.z - me.z;
                         const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
@@ -469,17 +519,16 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
                             ey = c.w * dy;
                             ez = c.w * dz;
                         }
-                        if (kPrec) {
-                            cells.add(inv3 * ex, inv3 * ey, inv3 * ez);
-                        } else {
-                            cells.ax = fmaf(inv3, ex, cells.ax);
-                            cells.ay = fmaf(inv3, ey, cells.ay);
-                            cells.az = fmaf(inv3, ez, cells.az);
-                        }
+                        rx = fmaf(inv3, ex, rx);
+                        ry = fmaf(inv3, ey, ry);
+                        rz = fmaf(inv3, ez, rz);
                     }
+                    if (kPrec) cells.add(px, py, pz);
                 }
-                inter += n_cell;
-                cell_inter += n_cell;
+                if (owner) {
+                    inter += n_cell;
+                    cell_inter += n_cell;
+                }
             }
             __syncwarp();
             n_cell = 0;
@@ -523,35 +572,51 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
                 __syncwarp();
                 const uint32_t cnt = min(32u, total - t0);
                 if (valid) {
+                    // Precision form, fast path: the tile's terms go into a
+                    // partial that is Kahan-added once.
+                    float px = 0.f, py = 0.f, pz = 0.f;
+                    float& rx = kPrec ? px : leaves.ax;
+                    float& ry = kPrec ? py : leaves.ay;
+                    float& rz = kPrec ? pz : leaves.az;
                     if (skip_self_free) {
                         // eps > 0: the self term is exactly zero, so no test is needed.
 #pragma unroll 4
-                        for (uint32_t q = 0; q < cnt; ++q) {
+                        for (uint32_t q = rep; q < cnt; q += reps) {
                             const float4 p = s_tile[warp][q];
                             const float dx = p.x - me.x, dy = p.y - me.y, dz = p.z - me.z;
                             const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
                             const float sc = p.w * (inv * inv * inv);
-                            if (kPrec) {
-                                leaves.add(dx * sc, dy * sc, dz * sc);
-                            } else {
-                                leaves.ax = fmaf(dx, sc, leaves.ax);
-                                leaves.ay = fmaf(dy, sc, leaves.ay);
-                                leaves.az = fmaf(dz, sc, leaves.az);
-                            }
+                            rx = fmaf(dx, sc, rx);
+                            ry = fmaf(dy, sc, ry);
+                            rz = fmaf(dz, sc, rz);
                         }
-                        inter += cnt;
-                    } else {
+                        if (owner) inter += cnt;
+                    } else if (kExact) {
                         for (uint32_t q = 0; q < cnt; ++q) {
+                            if (s_jdx[warp][q] != ip) {
+                                const float4 p = s_tile[warp][q];
+                                float tx, ty, tz;
+                                particle_term<true>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
+                                                    __fsub_rn(p.z, me.z), p.w, g, eps2, tx, ty, tz);
+                                leaves.push(tx, ty, tz);
+                                ++inter;
+                            }
+                            leaves.step();
+                        }
+                    } else {
+                        for (uint32_t q = rep; q < cnt; q += reps) {
                             if (s_jdx[warp][q] == ip) continue;
                             const float4 p = s_tile[warp][q];
                             float tx, ty, tz;
-                            particle_term<kExact>(__fsub_rn(p.x, me.x), __fsub_rn(p.y, me.y),
-                                                  __fsub_rn(p.z, me.z), p.w, kExact ? g : 1.0f, eps2,
-                                                  tx, ty, tz);
-                            leaves.add(tx, ty, tz);
+                            particle_term<false>(p.x - me.x, p.y - me.y, p.z - me.z, p.w, 1.0f, eps2,
+                                                 tx, ty, tz);
+                            rx += tx;
+                            ry += ty;
+                            rz += tz;
                             ++inter;
                         }
                     }
+                    if (kPrec && !kExact) leaves.add(px, py, pz);
                 }
             }
             __syncwarp();
@@ -587,7 +652,7 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
                 const bool leaf = has && !acc && (layer == 0 || r.w - r.z <= a.bucket);
                 const bool opn = has && !acc && !leaf;
                 const uint32_t tested = __popc(__ballot_sync(kFullMask, has));
-                if (valid) visits += tested;
+                if (owner) visits += tested;
                 // Accepted cells, in frontier order.
                 const uint32_t bacc = __ballot_sync(kFullMask, acc);
                 if (bacc) {
@@ -637,13 +702,39 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_group_kernel(TraverseArg
         flush_cells();
         flush_leaves();
         // The self-free fast loop counted the particle's own entry once.
-        if (!kExact && eps2 > 0.f && valid) --inter;
+        if (!kExact && eps2 > 0.f && owner) --inter;
 
-        if (valid) {
+        float sx, sy, sz;
+        if (kExact) {
+            cells.finish();
+            leaves.finish();
+            sx = __fadd_rn(cells.ax, leaves.ax);
+            sy = __fadd_rn(cells.ay, leaves.ay);
+            sz = __fadd_rn(cells.az, leaves.az);
+        } else {
+            // Compensated sums: the running sum minus its pending correction.
+            sx = (cells.ax - cells.cx) + (leaves.ax - leaves.cx);
+            sy = (cells.ay - cells.cy) + (leaves.ay - leaves.cy);
+            sz = (cells.az - cells.cz) + (leaves.az - leaves.cz);
+            if (reps > 1) {
+                __syncwarp();
+                if (valid) s_tile[warp][lane] = make_float4(sx, sy, sz, 0.f);
+                __syncwarp();
+                if (owner)
+                    for (uint32_t r = 1; r < reps; ++r) {
+                        const float4 t = s_tile[warp][lane + r * gcount];
+                        sx += t.x;
+                        sy += t.y;
+                        sz += t.z;
+                    }
+                __syncwarp();
+            }
+            sx *= g;
+            sy *= g;
+            sz *= g;
+        }
+        if (owner) {
             const float cl = a.clampv, dt = a.dt;
-            const float sx = kExact ? __fadd_rn(cells.ax, leaves.ax) : g * (cells.ax + leaves.ax);
-            const float sy = kExact ? __fadd_rn(cells.ay, leaves.ay) : g * (cells.ay + leaves.ay);
-            const float sz = kExact ? __fadd_rn(cells.az, leaves.az) : g * (cells.az + leaves.az);
             const float ax = fminf(fmaxf(sx, -cl), cl);
             const float ay = fminf(fmaxf(sy, -cl), cl);
             const float az = fminf(fmaxf(sz, -cl), cl);

@@ -21,6 +21,7 @@ does not shard); rank 0 prints the line with the max time over ranks.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -61,7 +62,7 @@ SEEDS = {"c1": 1001, "c2": 1002, "c3": 1003, "c4": 1004, "c5": 1005}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
@@ -104,25 +105,35 @@ def make_inputs(ic, workload):
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons; only the samples
+    taken between mark_start() and mark_end() (the timed region) count."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
+        self.window = None
+        self.lines = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)  # let the sampler start before the timed region
         except OSError:
             self.proc = None
         return self
+
+    def mark_start(self):
+        self._t0 = datetime.datetime.now()
+
+    def mark_end(self):
+        self.window = (self._t0, datetime.datetime.now())
 
     def __exit__(self, *exc):
         if self.proc:
@@ -133,28 +144,30 @@ class Clocks:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
             self.lines = [l for l in out.splitlines() if l.strip()]
-        else:
-            self.lines = []
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(f[2]), float(f[3]), f[6:10]))
             except ValueError:
                 continue
-            for name, v in zip(names, f[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(name)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = rows
+        if self.window:
+            lo, hi = self.window
+            inside = [r for r in rows if lo <= r[0] <= hi] or rows
+        reasons = {n for r in inside for n, v in zip(names, r[3]) if v.lower().startswith("active")}
+        return {"sm_mhz": float(np.median([r[1] for r in inside])), "sm_max_mhz": inside[-1][2],
+                "reasons": sorted(reasons), "samples": len(inside),
+                "window": "samples inside the timed region" if inside is not rows
+                          else "all samples (none fell inside the timed region)"}
 
 
 def measured_peaks():
@@ -188,6 +201,36 @@ def barrier(world: int):
         import torch.distributed as dist
 
         dist.barrier()
+
+
+def stage_bytes(n, key_bits, layer_counts, nsys, precision):
+    """Algorithmic HBM bytes of each stage of one PHYSICAL step.
+
+    bbox+encode: positions read twice (bbox, then encode) and the key written.
+    sort+reorder: 8 B/key for the histogram read, 24 B/key per 8-bit pass
+    (key and index read and written; 4 B less on the first pass, whose
+    indices are generated), then the reorder reads the permutation and
+    moves position, velocity and id (and the FP64 position).
+    build: keys read once by the topology pass, which writes two 4-byte
+    links per node; positions read once by the leaf pass; every node written
+    once (key 8, sums 16/32, centre of mass 16, ranges 16, quadrupole 20,
+    opening radius 4) and read once by its parent (sums, centre of mass,
+    quadrupole, range: 68/84).
+    integrate (kick-drift): position, velocity and acceleration read,
+    position and velocity written (plus the FP64 position read and written).
+    """
+    passes = (key_bits + 7) // 8
+    x64 = 24 if precision else 0
+    nodes = int(sum(layer_counts))
+    children = nodes - nsys
+    s_node = 8 + (32 if precision else 16) + 16 + 16 + 20 + 4
+    child_read = (32 if precision else 16) + 16 + 20 + 16
+    return {
+        "bbox+encode": (2 * (x64 or 16) + 8) * n,
+        "sort+reorder": (8 + 24 * passes - 4) * n + (4 + 2 * (16 + 16 + 4 + x64)) * n,
+        "build": (8 + 16 + x64) * n + nodes * (8 + s_node) + children * child_read,
+        "integrate": (80 + 2 * x64) * n,
+    }
 
 
 # ---------------------------------------------------------------- ours --
@@ -226,6 +269,7 @@ def run_ours(args, world, rank, local):
     barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
+        clk.mark_start()
         t0 = time.perf_counter()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
@@ -236,6 +280,7 @@ def run_ours(args, world, rank, local):
         sim.synchronize()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        clk.mark_end()
     barrier(world)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = sum(step_ms)
@@ -263,6 +308,44 @@ def run_ours(args, world, rank, local):
         stages[name] = ev[i].elapsed_time(ev[i + 1])
     interactions, visits, cell_inter = sim.read_stats(cells=True)
     sizes_, offsets, counts = sim.tree_info()
+    peaks, peak_src = measured_peaks()
+    key_bits = 3 * args.lbits + ((nsys - 1).bit_length() if nsys > 1 else 0)
+    sbytes = stage_bytes(n, key_bits, counts, nsys, form == L.FORM_PRECISION)
+    stage_roofline = {
+        k: {"bytes": int(b), "ms": stages[k], "achieved_gbs": b / (stages[k] * 1e-3) / 1e9,
+            "frac": b / (stages[k] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+        for k, b in sbytes.items()}
+
+    # The pair sort alone (astro_radix_sort) on uniform keys of the step's
+    # width and length, after an L2 flush: the sort stage's HBM roofline.
+    from astro_gb300.radix_sort import RadixSort
+
+    g = torch.Generator(device="cuda").manual_seed(SEEDS[args.workload])
+    keys = torch.randint(0, 1 << 62, (n,), device="cuda", generator=g, dtype=torch.int64)
+    if key_bits < 63:
+        keys &= (1 << key_bits) - 1
+    keys_out = torch.empty_like(keys)
+    idx_out = torch.empty(n, dtype=torch.int32, device="cuda")
+    sorter = RadixSort(n, key_bits)
+    sort_ms = []
+    for it in range(4):
+        with torch.cuda.stream(stream):
+            flush.fill_(3)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sorter.sort(keys, None, keys_out, idx_out, n, stream=sim.stream)
+            e1.record(stream)
+        sim.synchronize()
+        if it:
+            sort_ms.append(e0.elapsed_time(e1))
+    passes = (key_bits + 7) // 8
+    sort_b = (8 + 24 * passes - 4) * n
+    sort_roofline = {"bound": "hbm", "key_bits": key_bits, "passes": passes, "keys": n,
+                     "bytes": sort_b, "ms": float(np.mean(sort_ms)),
+                     "achieved": sort_b / (np.mean(sort_ms) * 1e-3) / 1e9,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": sort_b / (np.mean(sort_ms) * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+    del keys, keys_out, idx_out, sorter
     quad = (p.flags & L.FLAG_QUADRUPOLE) != 0
     flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * cell_inter + \
         FLOPS_PER_INTERACTION * (interactions - cell_inter)
@@ -284,7 +367,6 @@ def run_ours(args, world, rank, local):
         trav_ms.append(e0.elapsed_time(e1))
     trav = float(np.mean(trav_ms))
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    peaks, peak_src = measured_peaks()
     fp32_peak = 2 * 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     achieved = flops / (trav * 1e-3) / 1e12
 
@@ -369,7 +451,8 @@ def run_ours(args, world, rank, local):
                 counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
                 fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
                 launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr,
-                one_at_a_time=one_at_a_time)
+                one_at_a_time=one_at_a_time, stage_roofline=stage_roofline,
+                sort_roofline=sort_roofline)
 
 
 # ----------------------------------------------------------- CPU side --
@@ -468,10 +551,13 @@ def main():
             "data": "synthetic (seeded, Philox4x32-10)",
             "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"]),
             "e2e": r["e2e"], "gpu_launches": r["launches"],
-            "roofline": {"kernel": "traverse_phys_kernel", "bound": "fp32",
+            "roofline": {"kernel": ("traverse_group_kernel" if args.walk == "group"
+                                    else "traverse_phys_kernel"),
+                         "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
                          "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
                          "flops_per_launch": r["flops"],
+                         "interactions_per_s": r["interactions"] / (r["trav_ms"] * 1e-3),
                          "launch_ms": r["trav_ms"],
                          "peak_source": f"2 x 128 FP32 lanes x SMs x sm_max_mhz ({r['peak_src']} peaks file)"},
             "cpu_baseline": cpu, "clocks": r["clocks"],
@@ -481,7 +567,8 @@ def main():
             "interactions_per_particle": r["interactions"] / r["n"],
             "cell_interactions_per_particle": r["cell_inter"] / r["n"],
             "node_visits_per_particle": r["visits"] / r["n"],
-            "stages_ms": r["stages"], "layer_counts": r["counts"],
+            "stages_ms": r["stages"], "stage_roofline_hbm": r["stage_roofline"],
+            "sort_roofline": r["sort_roofline"], "layer_counts": r["counts"],
             "systems_one_at_a_time": r["one_at_a_time"],
         }
         print(json.dumps(line))

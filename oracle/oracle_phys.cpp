@@ -344,6 +344,39 @@ struct PhysState {
         }
     };
 
+    // Blocked compensated sum of the group walk: terms are added plainly
+    // within blocks of kBlock consecutive list positions, and each block's
+    // partial is Kahan-added to the running sum. Every list position
+    // counts, including a particle's own (skipped) position in the leaf
+    // list, so block boundaries depend on positions only. Without Kahan
+    // every term goes straight into the sum.
+    struct BlockAcc {
+        static constexpr uint32_t kBlock = 32;
+        float s[3] = {0, 0, 0}, c[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+        uint32_t k = 0;
+        void close() {
+            for (int a = 0; a < 3; ++a) {
+                float y = b[a] - c[a];
+                float u = s[a] + y;
+                c[a] = (u - s[a]) - y;
+                s[a] = u;
+                b[a] = 0.0f;
+            }
+        }
+        void add(bool kahan, const float t[3]) {
+            for (int a = 0; a < 3; ++a) {
+                if (kahan) b[a] += t[a];
+                else s[a] += t[a];
+            }
+        }
+        void step(bool kahan) {
+            if (kahan && ++k % kBlock == 0) close();
+        }
+        void finish(bool kahan) {
+            if (kahan && k % kBlock != 0) close();
+        }
+    };
+
     // Softened monopole of mass m at displacement d (r2t = |d|^2), plus the
     // quadrupole term of q = {Qxx, Qyy, Qxy, Qxz, Qyz} (Qzz = -Qxx - Qyy)
     // when q is not NULL:
@@ -522,7 +555,7 @@ struct PhysState {
             }
             for (uint32_t ip = gb; ip < ge; ++ip) {
                 const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
-                Acc A, B;
+                BlockAcc A, B;
                 float t[3];
                 uint64_t inter = 0;
                 for (uint32_t nd : cells) {
@@ -531,17 +564,22 @@ struct PhysState {
                     term(dx, dy, dz, dx * dx + dy * dy + dz * dz, c[3],
                          quad_on ? &quad[5ull * nd] : nullptr, t);
                     A.add(kahan, t);
+                    A.step(kahan);
                     ++inter;
                 }
+                A.finish(kahan);
                 for (uint32_t nd : leaves)
                     for (uint32_t j = pbeg[nd]; j < pend[nd]; ++j) {
-                        if (j == ip) continue;
-                        const float* q = &rel[4ull * j];
-                        float ex = q[0] - px, ey = q[1] - py, ez = q[2] - pz;
-                        term(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3], nullptr, t);
-                        B.add(kahan, t);
-                        ++inter;
+                        if (j != ip) {
+                            const float* q = &rel[4ull * j];
+                            float ex = q[0] - px, ey = q[1] - py, ez = q[2] - pz;
+                            term(ex, ey, ez, ex * ex + ey * ey + ez * ez, q[3], nullptr, t);
+                            B.add(kahan, t);
+                            ++inter;
+                        }
+                        B.step(kahan);
                     }
+                B.finish(kahan);
                 float a3[3] = {A.s[0] + B.s[0], A.s[1] + B.s[1], A.s[2] + B.s[2]};
                 finish(ip, a3);
                 tot_inter += inter;
