@@ -60,6 +60,11 @@ SIGNATURES = {
     "astro_read_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64),
                                  POINTER(c_uint64)]),
     "astro_direct_accel_f64": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
+    "astro_lighting": (c_int, [c_void_p, c_uint32]),
+    "astro_read_colors": (c_int, [c_void_p, c_void_p, c_uint32]),
+    "astro_save_state": (c_int, [c_void_p, c_char_p, c_uint64, c_double]),
+    "astro_load_state": (c_int, [c_char_p, c_uint32, POINTER(c_void_p), POINTER(c_uint64),
+                                 POINTER(c_double)]),
     "astro_get_stream": (c_int, [c_void_p, POINTER(c_void_p)]),
     "astro_last_error": (c_char_p, [c_void_p]),
     "astro_version": (c_char_p, []),

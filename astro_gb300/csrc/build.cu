@@ -424,8 +424,9 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
         }
         if (a.want_delta) a.node_crit2[j] = node_crit2(a, key, 0, cm);
         // A leaf holding more than one group is cut into group-sized chunks.
-        if (pe - pb > kGroupSize)
-            for (uint32_t b = pb; b < pe; b += kGroupSize) emit_group(a, b, min(b + kGroupSize, pe));
+        const uint32_t gs = a.group_size;
+        if (pe - pb > gs)
+            for (uint32_t b = pb; b < pe; b += gs) emit_group(a, b, min(b + gs, pe));
     }
 }
 
@@ -543,7 +544,8 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
         // Groups: a node over the group size packs runs of consecutive
         // small children (greedy, in child order); a small top-layer node is
         // a group by itself.
-        if (pe - pb > kGroupSize) {
+        const uint32_t gs = a.group_size;
+        if (pe - pb > gs) {
             uint2 cr[8];
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
@@ -555,11 +557,11 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
             for (uint32_t k = 0; k < 8; ++k) {
                 if (k >= nch) break;
                 const uint32_t cc = cr[k].y - cr[k].x;
-                if (cc <= kGroupSize) {
+                if (cc <= gs) {
                     if (ge == gb) {
                         gb = cr[k].x;
                         ge = cr[k].y;
-                    } else if ((ge - gb) + cc <= kGroupSize) {
+                    } else if ((ge - gb) + cc <= gs) {
                         ge = cr[k].y;
                     } else {
                         emit_group(a, gb, ge);
@@ -765,9 +767,60 @@ __global__ void gather_u32_kernel(const uint32_t* __restrict__ src, const uint32
 }
 
 __global__ void types_from_colors_kernel(const ColorType* __restrict__ ct, uint32_t* __restrict__ types,
-                                         uint32_t n) {
+                                         float4* __restrict__ colors, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) types[i] = ct[i].type;
+    if (i >= n) return;
+    types[i] = ct[i].type;
+    if (colors) colors[i] = *reinterpret_cast<const float4*>(&ct[i].color[0]);
+}
+
+// lightingPass (BarnesHut.metal:103-167) for the particles in upload order:
+// the lights' positions and colours (lights[0..nl) and lights[kMaxLights..])
+// were copied before the pass, so no light reads a colour written here.
+constexpr uint32_t kMaxLights = 5;
+constexpr float kLightAttenuation = 4e5f;  // LIGHT_ATTENUATION_DISTANCE, bridge.h:98
+
+__global__ void lights_snapshot_kernel(const float4* __restrict__ pos,
+                                       const float4* __restrict__ colors, float4* __restrict__ lights,
+                                       uint32_t nl) {
+    const uint32_t s = threadIdx.x;
+    if (s < nl) {
+        lights[s] = pos[s];
+        lights[kMaxLights + s] = colors[s];
+    }
+}
+
+__global__ void lighting_kernel(const float4* __restrict__ pos, const uint32_t* __restrict__ types,
+                                const float4* __restrict__ lights, float4* __restrict__ colors,
+                                uint32_t n, uint32_t nl) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t type = types[i];
+    if (type != 1u && type != 2u) return;
+    const float4 p = pos[i];
+    float lr = 0.f, lg = 0.f, lb = 0.f;
+    for (uint32_t s = 0; s < nl; ++s) {
+        const float4 q = lights[s], c = lights[kMaxLights + s];
+        const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+        const float dist =
+            __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        const float dn = fmaxf(__fdiv_rn(dist, kLightAttenuation), 1e-9f);
+        const float att = __fdiv_rn(1.0f, __fmul_rn(dn, dn));
+        lr = __fadd_rn(lr, __fmul_rn(c.x, att));
+        lg = __fadd_rn(lg, __fmul_rn(c.y, att));
+        lb = __fadd_rn(lb, __fmul_rn(c.z, att));
+    }
+    const float a = type == 2u ? fminf(fmaxf(lr, fmaxf(lg, lb)), 0.25f) : 1.0f;
+    colors[i] = make_float4(lr, lg, lb, a);
+}
+
+// ColorType in upload order from colours and types.
+__global__ void colors_out_kernel(const float4* __restrict__ colors, const uint32_t* __restrict__ types,
+                                  ColorType* __restrict__ out, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    *reinterpret_cast<float4*>(&out[i].color[0]) = colors[i];
+    *reinterpret_cast<uint4*>(&out[i].type) = make_uint4(types[i], 0u, 0u, 0u);
 }
 
 // Stand-alone PHYSICAL kick-drift (the same arithmetic as the traversal
@@ -957,9 +1010,25 @@ cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, uint32_t n,
+cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, float4* colors, uint32_t n,
                                      cudaStream_t st) {
-    types_from_colors_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ct, types, n);
+    types_from_colors_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ct, types, colors, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lighting(const float4* pos, const uint32_t* types, float4* colors, float4* lights,
+                            uint32_t n, uint32_t num_stars, cudaStream_t st) {
+    const uint32_t nl = std::min(std::min(num_stars, kMaxLights), n);
+    if (n == 0) return cudaSuccess;
+    if (nl > 0) lights_snapshot_kernel<<<1, 32, 0, st>>>(pos, colors, lights, nl);
+    lighting_kernel<<<blocks_for(n, 256), 256, 0, st>>>(pos, types, lights, colors, n, nl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_colors_out(const float4* colors, const uint32_t* types, ColorType* out, uint32_t n,
+                              cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    colors_out_kernel<<<blocks_for(n, 256), 256, 0, st>>>(colors, types, out, n);
     return cudaGetLastError();
 }
 

@@ -46,10 +46,11 @@ struct AggArgs {
     uint32_t want_quad;
     uint32_t want_delta;
     float theta;
+    uint32_t group_size;   // particles per group walk, 1..kGroupSize
     uint32_t* err;         // device error word (kErrBadLayer: a node with > 8 children)
 };
 
-constexpr uint32_t kGroupSize = 32;  // particles per group walk (one warp)
+constexpr uint32_t kGroupSize = 32;  // largest group of the group walk (one warp)
 
 struct DirectArgs {
     const float4* pos;
@@ -148,8 +149,13 @@ cudaError_t launch_direct_sum(const DirectArgs& a, cudaStream_t st);
 cudaError_t launch_inverse_ids(const uint32_t* ids, uint32_t* inv, uint32_t n, cudaStream_t st);
 cudaError_t launch_gather_u32(const uint32_t* src, const uint32_t* idx, uint32_t* dst, uint32_t n,
                               cudaStream_t st);
-cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, uint32_t n,
+cudaError_t launch_types_from_colors(const ColorType* ct, uint32_t* types, float4* colors, uint32_t n,
                                      cudaStream_t st);
+// Lighting pass; lights: 10 float4 of scratch (positions, colours).
+cudaError_t launch_lighting(const float4* pos, const uint32_t* types, float4* colors, float4* lights,
+                            uint32_t n, uint32_t num_stars, cudaStream_t st);
+cudaError_t launch_colors_out(const float4* colors, const uint32_t* types, ColorType* out, uint32_t n,
+                              cudaStream_t st);
 cudaError_t launch_kick_drift(bool prec, float4* pos, float4* vel, double* x64, const float4* acc,
                               uint32_t n, float dt, cudaStream_t st);
 

@@ -85,6 +85,11 @@ int validate_params(const astro_params* p, const char** why) {
         return (*why = "g and softening must be finite, softening >= 0", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->block_warps != 0 && p->block_warps != 2 && p->block_warps != 4 && p->block_warps != 8)
         return (*why = "block_warps must be 0, 2, 4 or 8", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->group_size > 32) return (*why = "group_size must be in [0, 32]", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->sort_variant > astro::sort_variant_count())
+        return (*why = "unknown sort_variant", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->light_sources > 0 && p->preset != ASTRO_PRESET_REFERENCE)
+        return (*why = "the lighting pass needs the REFERENCE preset", ASTRO_ERR_INVALID_ARGUMENT);
     return ASTRO_OK;
 }
 
@@ -223,7 +228,8 @@ int stage_sort(astro_ctx* ctx) {
     cudaStream_t st = ctx->stream;
     const uint32_t count = is_phys(ctx) ? ctx->n : ctx->n_tree;
     CK(astro::sort_pairs(ctx->codes, nullptr, ctx->sorted_keys, ctx->perm, count, nullptr,
-                         ctx->key_bits, ctx->sort_temp, ctx->sort_temp_bytes, st, ctx->err));
+                         ctx->key_bits, ctx->sort_temp, ctx->sort_temp_bytes, st, ctx->err,
+                         ctx->p.sort_variant));
     if (is_phys(ctx)) {
         if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "sort called twice without traverse");
         CK(astro::launch_reorder(is_prec(ctx), ctx->perm, ctx->pos[0], ctx->vel[0], ctx->ids[0],
@@ -277,6 +283,7 @@ int stage_build(astro_ctx* ctx) {
     a.want_quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.want_delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
     a.theta = ctx->p.theta;
+    a.group_size = ctx->p.group_size ? ctx->p.group_size : astro::kGroupSize;
     a.err = ctx->err;
     CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
     const int mode = !is_phys(ctx) ? 0 : (is_prec(ctx) ? 2 : 1);
@@ -381,6 +388,10 @@ int run_step(astro_ctx* ctx, float dt) {
     if ((r = stage_build(ctx)) != ASTRO_OK) return r;
     if (is_phys(ctx)) return stage_traverse(ctx, dt, true);
     if ((r = stage_traverse(ctx, 0.0f, false)) != ASTRO_OK) return r;
+    // barnesHut, lightingPass, updateSpheres (Renderer.swift:538-540).
+    if (ctx->p.light_sources > 0)
+        CK(astro::launch_lighting(ctx->pos[0], ctx->types, ctx->colors, ctx->lights, ctx->n,
+                                  ctx->p.light_sources, ctx->stream));
     return stage_integrate(ctx, dt);
 }
 
@@ -454,6 +465,7 @@ int astro_params_default(uint32_t preset, astro_params* out) {
         out->type_accel_scale[1] = 5.0f;
         out->type_accel_scale[2] = 1.0f;
         out->bucket = 0;
+        out->light_sources = 5;     // numStars (Renderer.swift:26)
     } else if (preset == ASTRO_PRESET_PHYSICAL) {
         out->g = 1.0f;
         out->softening = 0.01f;
@@ -500,6 +512,10 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     }
     CKC(dev_alloc(&ctx->acc, max_n));
     CKC(dev_alloc(&ctx->types, max_n));
+    if (params->preset == ASTRO_PRESET_REFERENCE) {
+        CKC(dev_alloc(&ctx->colors, max_n));
+        CKC(dev_alloc(&ctx->lights, 16));
+    }
     CKC(dev_alloc(&ctx->codes, max_n));
     CKC(dev_alloc(&ctx->sorted_keys, max_n));
     CKC(dev_alloc(&ctx->perm, max_n));
@@ -541,6 +557,8 @@ int astro_destroy(astro_ctx* ctx) {
     }
     dev_free(ctx->acc);
     dev_free(ctx->types);
+    dev_free(ctx->colors);
+    dev_free(ctx->lights);
     dev_free(ctx->codes);
     dev_free(ctx->sorted_keys);
     dev_free(ctx->perm);
@@ -588,6 +606,14 @@ int astro_set_params(astro_ctx* ctx, const astro_params* params) {
     const bool structural = params->preset != ctx->p.preset || params->form != ctx->p.form ||
                             params->lbits != ctx->p.lbits;
     if (params->form == ASTRO_FORM_PRECISION && (r = ensure_x64(ctx)) != ASTRO_OK) return r;
+    if (params->preset == ASTRO_PRESET_REFERENCE && !ctx->colors) {
+        if (dev_alloc(&ctx->colors, ctx->max_n) != cudaSuccess ||
+            dev_alloc(&ctx->lights, 16) != cudaSuccess) {
+            dev_free(ctx->colors);
+            dev_free(ctx->lights);
+            return fail(ctx, ASTRO_ERR_OUT_OF_MEMORY, "colour buffers");
+        }
+    }
     ctx->p = *params;
     drop_graph(ctx);
     if ((r = ensure_frontier(ctx)) != ASTRO_OK) return r;
@@ -670,8 +696,9 @@ static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityR
                                         n_tree, st));
         d_ct = reinterpret_cast<ColorType*>(stg);
         CK(cudaMemcpyAsync(d_ct, ct, sizeof(ColorType) * n, cudaMemcpyHostToDevice, st));
-        CK(astro::launch_types_from_colors(d_ct, ctx->types, n, st));
+        CK(astro::launch_types_from_colors(d_ct, ctx->types, ctx->colors, n, st));
     } else {
+        if (ctx->colors) CK(cudaMemsetAsync(ctx->colors, 0, sizeof(float4) * n, st));
         CK(astro::launch_upload_convert(prec, d_pm, d_vr, nullptr, ctx->pos[0], ctx->vel[0],
                                         phys ? ctx->ids[0] : nullptr, ctx->types, ctx->x64[0], n,
                                         n_tree, st));
@@ -929,6 +956,183 @@ int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t 
     CK(astro::launch_direct_sum(a, st));
     CK(cudaMemcpyAsync(acc3, d_out, 24ull * n_sample, cudaMemcpyDeviceToHost, st));
     return check_device(ctx);
+}
+
+int astro_lighting(astro_ctx* ctx, uint32_t num_stars) {
+    NEED_UPLOAD();
+    if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "lighting needs the REFERENCE preset");
+    CK(astro::launch_lighting(ctx->pos[0], ctx->types, ctx->colors, ctx->lights, ctx->n, num_stars,
+                              ctx->stream));
+    return ASTRO_OK;
+}
+
+int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n) {
+    NEED_UPLOAD();
+    if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "colours need the REFERENCE preset");
+    if (!ct || n != ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_colors: n mismatch");
+    ColorType* tmp = static_cast<ColorType*>(ctx->staging);
+    CK(astro::launch_colors_out(ctx->colors, ctx->types, tmp, n, ctx->stream));
+    CK(cudaMemcpyAsync(ct, tmp, sizeof(ColorType) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device(ctx);
+}
+
+// ------------------------------------------------------------ state files --
+
+}  // extern "C"
+
+namespace {
+
+struct File {
+    FILE* f = nullptr;
+    ~File() {
+        if (f) std::fclose(f);
+    }
+    bool put(const void* p, size_t n) { return n == 0 || std::fwrite(p, 1, n, f) == n; }
+    bool get(void* p, size_t n) { return n == 0 || std::fread(p, 1, n, f) == n; }
+};
+
+}  // namespace
+
+extern "C" {
+
+int astro_save_state(astro_ctx* ctx, const char* path, uint64_t step, double time) {
+    NEED_UPLOAD();
+    if (!path) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "save_state: path is NULL");
+    if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "save_state in the middle of a step");
+    const uint32_t n = ctx->n;
+    cudaStream_t st = ctx->stream;
+    const Cur c = current(ctx);
+    const bool has_types = !is_phys(ctx), has64 = is_prec(ctx);
+    std::vector<float4> pos(n), vel(n);
+    std::vector<uint32_t> ids(n), types(has_types ? n : 0);
+    std::vector<double> soa(has64 ? 3ull * n : 0);
+    CK(cudaMemcpyAsync(pos.data(), c.pos, 16ull * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(vel.data(), c.vel, 16ull * n, cudaMemcpyDeviceToHost, st));
+    if (c.ids) CK(cudaMemcpyAsync(ids.data(), c.ids, 4ull * n, cudaMemcpyDeviceToHost, st));
+    else
+        for (uint32_t i = 0; i < n; ++i) ids[i] = i;
+    if (has_types) CK(cudaMemcpyAsync(types.data(), ctx->types, 4ull * n, cudaMemcpyDeviceToHost, st));
+    if (has64) CK(cudaMemcpyAsync(soa.data(), c.x64, 24ull * n, cudaMemcpyDeviceToHost, st));
+    int r = check_device(ctx);
+    if (r != ASTRO_OK) return r;
+    std::vector<PositionMass> pm(n);
+    std::vector<VelocityRadius> vr(n);
+    std::vector<double> xyz(has64 ? 3ull * n : 0);
+    std::memset(pm.data(), 0, sizeof(PositionMass) * n);
+    std::memset(vr.data(), 0, sizeof(VelocityRadius) * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        pm[i].position[0] = pos[i].x;
+        pm[i].position[1] = pos[i].y;
+        pm[i].position[2] = pos[i].z;
+        pm[i].mass = pos[i].w;
+        vr[i].velocity[0] = vel[i].x;
+        vr[i].velocity[1] = vel[i].y;
+        vr[i].velocity[2] = vel[i].z;
+        vr[i].radius = vel[i].w;
+        if (has64)
+            for (int a = 0; a < 3; ++a) {
+                xyz[3ull * i + a] = soa[(size_t)a * n + i];
+                pm[i].position[a] = (float)soa[(size_t)a * n + i];
+            }
+    }
+    astro_state_header h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, ASTRO_STATE_MAGIC, 8);
+    h.version = ASTRO_STATE_VERSION;
+    h.header_bytes = sizeof(h);
+    h.params = ctx->p;
+    h.step = step;
+    h.time = time;
+    h.n = n;
+    h.n_tree = ctx->n_tree;
+    h.nsys = ctx->nsys;
+    h.contents = (has_types ? ASTRO_STATE_TYPES : 0u) | (has64 ? ASTRO_STATE_POS64 : 0u);
+    File f;
+    f.f = std::fopen(path, "wb");
+    if (!f.f) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "save_state: cannot open the file");
+    bool ok = f.put(&h, sizeof(h)) && f.put(ctx->sys_sizes.data(), 4ull * ctx->nsys) &&
+              f.put(pm.data(), sizeof(PositionMass) * n) && f.put(vr.data(), sizeof(VelocityRadius) * n) &&
+              f.put(ids.data(), 4ull * n) && f.put(types.data(), 4ull * types.size()) &&
+              f.put(xyz.data(), 8ull * xyz.size());
+    ok = (std::fclose(f.f) == 0) && ok;
+    f.f = nullptr;
+    if (!ok) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "save_state: write failed");
+    return ASTRO_OK;
+}
+
+int astro_load_state(const char* path, uint32_t max_n, astro_ctx** out, uint64_t* step,
+                     double* time) {
+    if (!path || !out) return ASTRO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    File f;
+    f.f = std::fopen(path, "rb");
+    if (!f.f) return ASTRO_ERR_INVALID_ARGUMENT;
+    astro_state_header h;
+    if (!f.get(&h, sizeof(h)) || std::memcmp(h.magic, ASTRO_STATE_MAGIC, 8) != 0 ||
+        h.version != ASTRO_STATE_VERSION || h.header_bytes != sizeof(h) || h.n == 0 ||
+        h.nsys == 0 || h.n_tree > h.n || (h.contents & ~(ASTRO_STATE_TYPES | ASTRO_STATE_POS64)))
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    const char* why = nullptr;
+    if (validate_params(&h.params, &why) != ASTRO_OK) return ASTRO_ERR_INVALID_ARGUMENT;
+    const bool phys = h.params.preset == ASTRO_PRESET_PHYSICAL;
+    const bool prec = phys && h.params.form == ASTRO_FORM_PRECISION;
+    if (((h.contents & ASTRO_STATE_TYPES) != 0) == phys ||
+        ((h.contents & ASTRO_STATE_POS64) != 0) != prec || (!phys && h.nsys != 1))
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    const uint32_t n = h.n;
+    std::vector<uint32_t> sizes(h.nsys), ids(n), types(phys ? 0 : n);
+    std::vector<PositionMass> pm(n);
+    std::vector<VelocityRadius> vr(n);
+    std::vector<double> xyz(prec ? 3ull * n : 0);
+    if (!f.get(sizes.data(), 4ull * h.nsys) || !f.get(pm.data(), sizeof(PositionMass) * n) ||
+        !f.get(vr.data(), sizeof(VelocityRadius) * n) || !f.get(ids.data(), 4ull * n) ||
+        !f.get(types.data(), 4ull * types.size()) || !f.get(xyz.data(), 8ull * xyz.size()))
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    uint64_t total = 0;
+    for (uint32_t s : sizes) total += s;
+    if (phys ? total != n : sizes[0] != h.n_tree) return ASTRO_ERR_INVALID_ARGUMENT;
+    // ids must be a permutation of 0..n-1.
+    {
+        std::vector<uint8_t> seen(n, 0);
+        for (uint32_t i : ids) {
+            if (i >= n || seen[i]) return ASTRO_ERR_INVALID_ARGUMENT;
+            seen[i] = 1;
+        }
+    }
+    astro_ctx* ctx = nullptr;
+    int r = astro_create(&h.params, std::max(max_n, n), h.nsys, &ctx);
+    if (r != ASTRO_OK) return r;
+    if (!phys) {
+        std::vector<ColorType> ct(n);
+        std::memset(ct.data(), 0, sizeof(ColorType) * n);
+        for (uint32_t i = 0; i < n; ++i) ct[i].type = types[i];
+        r = astro_upload(ctx, pm.data(), vr.data(), ct.data(), n, h.n_tree);
+    } else if (h.nsys == 1) {
+        r = astro_upload(ctx, pm.data(), vr.data(), nullptr, n, n);
+    } else {
+        r = astro_upload_systems(ctx, pm.data(), vr.data(), sizes.data(), h.nsys);
+    }
+    if (r == ASTRO_OK && phys) {
+        // The saved slot order and upload indices; the FP64 master positions.
+        cudaStream_t st = ctx->stream;
+        cudaError_t e = cudaMemcpyAsync(ctx->ids[0], ids.data(), 4ull * n, cudaMemcpyHostToDevice, st);
+        std::vector<double> soa(prec ? 3ull * n : 0);
+        for (uint32_t i = 0; i < n && prec; ++i)
+            for (int a = 0; a < 3; ++a) soa[(size_t)a * n + i] = xyz[3ull * i + a];
+        if (e == cudaSuccess && prec)
+            e = cudaMemcpyAsync(ctx->x64[0], soa.data(), 24ull * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = fail(ctx, ASTRO_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (r == ASTRO_OK) r = check_device(ctx);
+    if (r != ASTRO_OK) {
+        astro_destroy(ctx);
+        return r;
+    }
+    if (step) *step = h.step;
+    if (time) *time = h.time;
+    *out = ctx;
+    return ASTRO_OK;
 }
 
 }  // extern "C"

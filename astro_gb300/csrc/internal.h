@@ -52,10 +52,13 @@ cudaError_t sort_init();
 // Stable sort of n_est (key, value) pairs (count read from d_count when not
 // NULL). vals_in NULL => values are 0..n-1. err (device word) collects
 // look-back timeouts; NULL => the word inside temp.
+// variant: 0 = the library default, 1..sort_variant_count() = a pass kernel
+// of the astro_params.sort_variant table.
 cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                        uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
                        uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
-                       uint32_t* err);
+                       uint32_t* err, uint32_t variant = 0);
+uint32_t sort_variant_count();
 
 // ------------------------------------------------------------ pipeline ----
 struct DeviceState;  // defined in context.cu
@@ -87,6 +90,8 @@ struct astro_ctx {
     uint32_t* ids[2] = {nullptr, nullptr};
     double* x64[2] = {nullptr, nullptr};  // SoA x | y | z, precision form
     float4* acc = nullptr;
+    float4* colors = nullptr;         // REFERENCE: ColorType colours (lighting pass)
+    float4* lights = nullptr;         // REFERENCE: lighting pass light snapshot
     uint32_t* types = nullptr;
     uint64_t* codes = nullptr;        // keys in the state order before sorting
     uint64_t* sorted_keys = nullptr;

@@ -313,6 +313,8 @@ cudaError_t sort_init() {
     return e;
 }
 
+uint32_t sort_variant_count() { return (uint32_t)kNumVariants; }
+
 SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
     SortPlan p{};
     p.passes = key_bits == 0 ? 1u : (key_bits + 7u) / 8u;
@@ -340,13 +342,14 @@ SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
 cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                        uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
                        uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
-                       uint32_t* err) {
+                       uint32_t* err, uint32_t variant) {
     if (n_est == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(n_est, key_bits);
-    if (temp_bytes < plan.total || key_bits > 64) return cudaErrorInvalidValue;
+    if (temp_bytes < plan.total || key_bits > 64 || variant > (uint32_t)kNumVariants)
+        return cudaErrorInvalidValue;
     cudaError_t e0 = sort_init();
     if (e0 != cudaSuccess) return e0;
-    const PassVariant& pv = kVariants[g_variant];
+    const PassVariant& pv = kVariants[variant == 0 ? g_variant : (int)variant - 1];
     const uint32_t tile = (uint32_t)(kThreads * pv.items);
     const uint32_t ntiles = (uint32_t)(((uint64_t)n_est + tile - 1) / tile);
     char* base = static_cast<char*>(temp);

@@ -72,7 +72,10 @@ class Params(ctypes.Structure):
         ("type_accel_scale", ctypes.c_float * 3),
         ("bucket", ctypes.c_uint32),
         ("block_warps", ctypes.c_uint32),
-        ("_reserved", ctypes.c_uint32 * 6),
+        ("group_size", ctypes.c_uint32),
+        ("sort_variant", ctypes.c_uint32),
+        ("light_sources", ctypes.c_uint32),
+        ("_reserved", ctypes.c_uint32 * 3),
     ]
 
     def replace(self, **kw) -> "Params":
@@ -94,3 +97,55 @@ class Params(ctypes.Structure):
 def empty_particles(n: int):
     """Zeroed PositionMass and VelocityRadius arrays of length n."""
     return np.zeros(n, POSITION_MASS), np.zeros(n, VELOCITY_RADIUS)
+
+
+STATE_MAGIC = b"ASTROST1"
+STATE_VERSION = 1
+STATE_TYPES = 0x1
+STATE_POS64 = 0x2
+
+
+class StateHeader(ctypes.Structure):
+    """astro_state_header: the fixed part of a state file."""
+
+    _fields_ = [
+        ("magic", ctypes.c_char * 8),
+        ("version", ctypes.c_uint32),
+        ("header_bytes", ctypes.c_uint32),
+        ("params", Params),
+        ("step", ctypes.c_uint64),
+        ("time", ctypes.c_double),
+        ("n", ctypes.c_uint32),
+        ("n_tree", ctypes.c_uint32),
+        ("nsys", ctypes.c_uint32),
+        ("contents", ctypes.c_uint32),
+    ]
+
+
+def read_state(path):
+    """Parse a state file on the host: (header, sys_sizes, pm, vr, ids, types
+    or None, pos64 or None), arrays in the saved slot order."""
+    import numpy as np
+
+    raw = open(path, "rb").read()
+    h = StateHeader.from_buffer_copy(raw[:ctypes.sizeof(StateHeader)])
+    if h.magic != STATE_MAGIC or h.version != STATE_VERSION:
+        raise ValueError("not an astro state file")
+    off = h.header_bytes
+    n = h.n
+
+    def take(dtype, count):
+        nonlocal off
+        a = np.frombuffer(raw, dtype=dtype, count=count, offset=off).copy()
+        off += a.nbytes
+        return a
+
+    sizes = take(np.uint32, h.nsys)
+    pm = take(POSITION_MASS, n)
+    vr = take(VELOCITY_RADIUS, n)
+    ids = take(np.uint32, n)
+    types = take(np.uint32, n) if h.contents & STATE_TYPES else None
+    pos64 = take(np.float64, 3 * n).reshape(n, 3) if h.contents & STATE_POS64 else None
+    if off != len(raw):
+        raise ValueError("state file size does not match its header")
+    return h, sizes, pm, vr, ids, types, pos64

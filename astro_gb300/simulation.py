@@ -93,6 +93,29 @@ class Simulation:
         self._check(lib().astro_download(self._h, ptr(pm), ptr(vr), self.n))
         return pm, vr
 
+    # -- state files (makeSpheres / resetSimulation without regeneration) --
+    def save_state(self, path, step: int = 0, time: float = 0.0) -> None:
+        """Write the state between steps (include/astro_cuda.h: state files)."""
+        self._check(lib().astro_save_state(self._h, str(path).encode(), step, time))
+
+    @classmethod
+    def load_state(cls, path, max_n: int = 0) -> tuple["Simulation", int, float]:
+        """A new context restored from a state file, with the saved step
+        count and time."""
+        h = c_void_p()
+        step, t = c_uint64(), ctypes.c_double()
+        check(lib().astro_load_state(str(path).encode(), max_n, byref(h), byref(step), byref(t)))
+        sim = cls.__new__(cls)
+        sim._h = h
+        p = L.Params()
+        sim._check(lib().astro_get_params(h, byref(p)))
+        hdr, sizes, *_ = L.read_state(path)
+        sim.params = p
+        sim.max_n = max(max_n, hdr.n)
+        sim.n, sim.n_tree = hdr.n, hdr.n_tree
+        sim.sys_sizes = [int(s) for s in sizes]
+        return sim, step.value, t.value
+
     # -- stages (Renderer.draw order) -------------------------------------
     def generate_morton_codes(self) -> None:
         self._check(lib().astro_encode(self._h))
@@ -108,6 +131,16 @@ class Simulation:
 
     def update_spheres(self, dt: float) -> None:
         self._check(lib().astro_integrate(self._h, dt))
+
+    def lighting_pass(self, num_stars: int = 5) -> None:
+        """lightingPass (BarnesHut.metal:103-167), REFERENCE preset."""
+        self._check(lib().astro_lighting(self._h, num_stars))
+
+    def read_colors(self) -> np.ndarray:
+        """ColorType of every particle in upload order (REFERENCE preset)."""
+        ct = np.zeros(self.n, L.COLOR_TYPE)
+        self._check(lib().astro_read_colors(self._h, ptr(ct), self.n))
+        return ct
 
     def draw(self, dt: float, steps: int = 1) -> None:
         """Run `steps` full steps (graph-replayed unless FLAG_NO_GRAPH)."""

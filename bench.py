@@ -34,6 +34,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from astro_gb300.workloads import WORKLOADS  # noqa: E402  (no CUDA needed to import)
+
 METRIC = "particle-updates/s per GB300 step (plain FP32 vs precision+batched) at stated FP64 error"
 UNIT = "particle-updates/s"
 # Flops per interaction: 20 for a softened particle-particle or monopole term
@@ -44,21 +46,6 @@ FLOPS_PER_INTERACTION = 20
 FLOPS_PER_QUAD_CELL = 50
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
-WORKLOADS = {
-    # name: (description, generator, n, params overrides, dt)
-    "c1": ("Plummer sphere a=1 N=16384", "plummer", 16384, dict(softening=0.01), 1e-3),
-    "c2": ("exponential disk + Hernquist bulge N=524288", "disk_bulge", 524288,
-           dict(softening=0.005), 5e-4),
-    "c3": ("two Plummer spheres a=1 M=0.5 at separation 10, N=4194304", "two_plummer", 4194304,
-           dict(softening=0.002), 1e-3),
-    "c4": ("256 Plummer systems, N_s log-uniform [1024, 65536]", "batch", 0,
-           dict(softening=0.01), 1e-3),
-    "c5": ("uniform unit cube, log-normal masses, N=16777216", "uniform_cube", 16777216,
-           dict(softening=0.001), 1e-3),
-}
-SEEDS = {"c1": 1001, "c2": 1002, "c3": 1003, "c4": 1004, "c5": 1005}
-
-
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -67,10 +54,15 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--form", choices=["plain", "precision"], default="plain")
-    ap.add_argument("--lbits", type=int, default=14)
+    # Launch knobs: unset ones come from the autotuner's file for the
+    # workload and form (astro_gb300/tuned.json), else the preset defaults.
+    ap.add_argument("--lbits", type=int, default=None)
+    ap.add_argument("--bucket", type=int, default=None)
+    ap.add_argument("--warps", type=int, default=None)
+    ap.add_argument("--group-size", type=int, default=None)
+    ap.add_argument("--sort-variant", type=int, default=None)
+    ap.add_argument("--no-tuned", action="store_true", help="ignore the autotuner's file")
     ap.add_argument("--theta", type=float, default=0.7)
-    ap.add_argument("--bucket", type=int, default=16)
-    ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--persistent", action="store_true")
     ap.add_argument("--walk", choices=["group", "particle"], default="group")
     ap.add_argument("--monopole", action="store_true",
@@ -95,13 +87,34 @@ def walk_flags(args, L, flags):
     return flags
 
 
-def make_inputs(ic, workload):
-    _, gen, n, _, _ = WORKLOADS[workload]
-    seed = SEEDS[workload]
-    if gen == "batch":
-        pm, vr, sizes = ic.plummer_batch(256, seed)
-        return pm, vr, [int(s) for s in sizes]
-    return getattr(ic, gen)(n, seed) + (None,)
+def knobs(args):
+    """Launch knobs: command line, else the tuned file, else the defaults."""
+    tuned = {}
+    if not args.no_tuned:
+        from astro_gb300 import autotune
+
+        tuned = autotune.load().get(f"{args.workload}/{args.form}", {}).get("knobs", {})
+    default = {"lbits": WORKLOADS[args.workload].lbits, "bucket": 16, "block_warps": 0,
+               "group_size": 0, "sort_variant": 0}
+    given = {"lbits": args.lbits, "bucket": args.bucket, "block_warps": args.warps,
+             "group_size": args.group_size, "sort_variant": args.sort_variant}
+    out, source = {}, {}
+    for k in default:
+        if given[k] is not None:
+            out[k], source[k] = given[k], "command line"
+        elif k in tuned:
+            out[k], source[k] = tuned[k], "autotuner"
+        else:
+            out[k], source[k] = default[k], "default"
+    return out, source
+
+
+def make_params(args, ag, L):
+    w = WORKLOADS[args.workload]
+    form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
+    k, source = knobs(args)
+    p = ag.default_params(L.PRESET_PHYSICAL, theta=args.theta, form=form, **k, **w.physics)
+    return p.replace(flags=walk_flags(args, L, p.flags)), source
 
 
 class Clocks:
@@ -243,13 +256,12 @@ def run_ours(args, world, rank, local):
     from astro_gb300 import layouts as L
 
     torch.cuda.set_device(local)
-    desc, _, _, over, dt = WORKLOADS[args.workload]
-    pm, vr, sizes = make_inputs(ic, args.workload)
+    w = WORKLOADS[args.workload]
+    desc, dt = w.description, w.dt
+    pm, vr, sizes = w.make()
     n = len(pm)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
-    p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
-                          bucket=args.bucket, block_warps=args.warps, form=form, **over)
-    p = p.replace(flags=walk_flags(args, L, p.flags))
+    p, knob_source = make_params(args, ag, L)
     nsys = len(sizes) if sizes else 1
     sim = ag.Simulation(p, max_n=n, max_systems=nsys)
     upload = (lambda: sim.upload_systems(pm, vr, sizes)) if sizes else (lambda: sim.upload(pm, vr))
@@ -309,7 +321,7 @@ def run_ours(args, world, rank, local):
     interactions, visits, cell_inter = sim.read_stats(cells=True)
     sizes_, offsets, counts = sim.tree_info()
     peaks, peak_src = measured_peaks()
-    key_bits = 3 * args.lbits + ((nsys - 1).bit_length() if nsys > 1 else 0)
+    key_bits = 3 * p.lbits + ((nsys - 1).bit_length() if nsys > 1 else 0)
     sbytes = stage_bytes(n, key_bits, counts, nsys, form == L.FORM_PRECISION)
     stage_roofline = {
         k: {"bytes": int(b), "ms": stages[k], "achieved_gbs": b / (stages[k] * 1e-3) / 1e9,
@@ -320,7 +332,7 @@ def run_ours(args, world, rank, local):
     # width and length, after an L2 flush: the sort stage's HBM roofline.
     from astro_gb300.radix_sort import RadixSort
 
-    g = torch.Generator(device="cuda").manual_seed(SEEDS[args.workload])
+    g = torch.Generator(device="cuda").manual_seed(w.seed)
     keys = torch.randint(0, 1 << 62, (n,), device="cuda", generator=g, dtype=torch.int64)
     if key_bits < 63:
         keys &= (1 << key_bits) - 1
@@ -371,7 +383,7 @@ def run_ours(args, world, rank, local):
     achieved = flops / (trav * 1e-3) / 1e12
 
     # Error against the FP64 direct sum on sampled particles (current state).
-    rng = np.random.default_rng(SEEDS[args.workload])
+    rng = np.random.default_rng(w.seed)
     samples = np.sort(rng.choice(n, size=min(args.error_samples, n), replace=False)).astype(np.uint32)
     sim.generate_morton_codes()
     sim.sort()
@@ -442,10 +454,11 @@ def run_ours(args, world, rank, local):
         for s1 in sims:
             s1.close()
 
-    passes = (3 * args.lbits + (int(np.ceil(np.log2(nsys))) if nsys > 1 else 0) + 7) // 8
-    launches_per_step = 7 + passes + (args.lbits + 1)
+    passes = (key_bits + 7) // 8
+    launches_per_step = 7 + passes + (p.lbits + 1)
     sim.close()
-    return dict(n=n, desc=desc, dt=dt, p=p, value=value, t_ms=t_ms_max, wall=wall,
+    return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
+                wall=wall,
                 step_ms=step_ms, stages=stages, interactions=interactions, visits=visits,
                 cell_inter=cell_inter, flops=flops,
                 counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
@@ -484,13 +497,12 @@ def run_reference(args):
     from astro_gb300 import layouts as L
     from oracle import oracle as orc
 
-    desc, _, _, over, dt = WORKLOADS[args.workload]
-    pm, vr, sizes = make_inputs(ic, args.workload)
+    w = WORKLOADS[args.workload]
+    desc, dt = w.description, w.dt
+    pm, vr, sizes = w.make()
     n = len(pm)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
-    p = ag.default_params(L.PRESET_PHYSICAL, lbits=args.lbits, theta=args.theta,
-                          bucket=args.bucket, form=form, **over)
-    p = p.replace(flags=walk_flags(args, L, p.flags))
+    p, knob_source = make_params(args, ag, L)
     cores = orc.set_threads(0)
     pm_c, vr_c = pm.copy(), vr.copy()
     for _ in range(args.warmup):
@@ -506,20 +518,22 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if form == 0 else "f32+f64",
         "data": "synthetic (seeded, Philox4x32-10)", "impl": "reference",
-        "config": config_dict(args, desc, n, dt, p),
+        "config": config_dict(args, desc, n, dt, p, knob_source),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
-def config_dict(args, desc, n, dt, p):
+def config_dict(args, desc, n, dt, p, knob_source):
     walk = "per-particle" if p.flags & 0x20 else "group"
     return {"workload": f"{args.workload}: {desc}", "n": n, "preset": "PHYSICAL",
             "form": args.form, "walk": walk, "quadrupole": bool(p.flags & 0x10),
             "opening": "size/theta + delta" if p.flags & 0x8 else "size/theta",
-            "lbits": p.lbits, "theta": p.theta, "eps": p.softening,
-            "dt": dt, "bucket": p.bucket, "G": p.g,
+            "theta": p.theta, "eps": p.softening, "dt": dt, "G": p.g,
+            "lbits": p.lbits, "bucket": p.bucket, "group_size": p.group_size or 32,
+            "block_warps": p.block_warps or 4, "sort_variant": p.sort_variant,
+            "knob_source": knob_source,
             "l2": "flushed (256 MB write) before every timed step",
             "parallelism": "replicas (one independent system per GPU)"}
 
@@ -549,7 +563,7 @@ def main():
             "ms_per_step": r["t_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.form == "plain" else "f32+f64",
             "data": "synthetic (seeded, Philox4x32-10)",
-            "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"]),
+            "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"], r["knob_source"]),
             "e2e": r["e2e"], "gpu_launches": r["launches"],
             "roofline": {"kernel": ("traverse_group_kernel" if args.walk == "group"
                                     else "traverse_phys_kernel"),

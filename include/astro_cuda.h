@@ -170,7 +170,19 @@ typedef struct astro_params {
                                  particles is summed particle by particle
                                  (0 = only at layer 0) */
     uint32_t block_warps;     /* traversal: warps per block (0 = autotuned/default) */
-    uint32_t _reserved[6];
+    uint32_t group_size;      /* PHYSICAL group walk: at most this many consecutive
+                                 particles share one tree walk (one warp), 1..32;
+                                 0 = 32 */
+    uint32_t sort_variant;    /* radix sort pass kernel (items per thread / blocks
+                                 per SM / ranking): 0 = library default,
+                                 1 = 16/2/ballot, 2 = 16/2/match, 3 = 12/3/match,
+                                 4 = 8/4/match, 5 = 20/2/match, 6 = 12/3/ballot,
+                                 7 = 8/4/ballot */
+    uint32_t light_sources;   /* REFERENCE: astro_step runs the lighting pass
+                                 with the first light_sources particles (at most
+                                 5) as lights (Renderer.swift:539; numStars = 5);
+                                 0 = no lighting pass */
+    uint32_t _reserved[3];
 } astro_params;
 
 /* Fill *out with the defaults of a preset. */
@@ -246,6 +258,63 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
  * on the device from the current positions. acc3 holds 3 doubles per sample. */
 int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t n_sample,
                            double* acc3);
+
+/* Lighting pass (BarnesHut.metal:103-167), REFERENCE preset: every planet
+ * (type 1) and dust particle (type 2) takes the light of the first
+ * min(num_stars, 5) particles,
+ *   rgb = sum_s rgb_s / max(|x_s - x| / 4e5, 1e-9)^2   (bridge.h:98),
+ *   alpha = 1 for planets, min(max(r, g, b), 0.25) for dust;
+ * stars keep their colour. The lights' positions and colours are taken before
+ * the pass writes any colour. Colours are the ColorType values of the upload
+ * (zero when none were given). */
+int astro_lighting(astro_ctx* ctx, uint32_t num_stars);
+/* ColorType of every particle (colour after the last lighting pass, type) in
+ * upload order. */
+int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n);
+
+/* ---------------------------------------------------------------------------
+ * State files: the role of makeSpheres / resetSimulation
+ * (Renderer.swift:148-152,441-493) for a headless step loop, which the
+ * reference rebuilds from an unseeded generator on every reset.
+ *
+ * A state file (little-endian) is an astro_state_header followed by
+ *   uint32_t       sys_sizes[nsys]
+ *   PositionMass   pm[n]      particles in the context's current slot order
+ *   VelocityRadius vr[n]
+ *   uint32_t       ids[n]     upload index of each slot
+ *   uint32_t       types[n]   if contents & ASTRO_STATE_TYPES (REFERENCE preset)
+ *   double         pos64[3n]  if contents & ASTRO_STATE_POS64 (precision form;
+ *                             x, y, z per particle)
+ * Loading restores the slot order, so a loaded context's next steps are
+ * bit-identical to the saved context's. Colours are not state (only the type
+ * is): a loaded REFERENCE context has type-only ColorType values.
+ * ------------------------------------------------------------------------- */
+#define ASTRO_STATE_MAGIC "ASTROST1"
+#define ASTRO_STATE_VERSION 1u
+#define ASTRO_STATE_TYPES 0x1u
+#define ASTRO_STATE_POS64 0x2u
+
+typedef struct astro_state_header {
+    char magic[8];            /* ASTRO_STATE_MAGIC, not NUL-terminated */
+    uint32_t version;         /* ASTRO_STATE_VERSION */
+    uint32_t header_bytes;    /* sizeof(astro_state_header) */
+    astro_params params;
+    uint64_t step;            /* caller's step counter */
+    double time;              /* caller's simulated time */
+    uint32_t n;
+    uint32_t n_tree;
+    uint32_t nsys;
+    uint32_t contents;        /* ASTRO_STATE_* */
+} astro_state_header;
+
+/* Write the context's state (between steps) with the caller's step count and
+ * time. */
+int astro_save_state(astro_ctx* ctx, const char* path, uint64_t step, double time);
+/* Create a context for at least max_n particles (0: exactly the file's) from
+ * a state file and restore its state; *step and *time (may be NULL) receive
+ * the saved counters. */
+int astro_load_state(const char* path, uint32_t max_n, astro_ctx** out, uint64_t* step,
+                     double* time);
 
 /* Device pointer access for callers that own their own kernels. */
 int astro_get_stream(astro_ctx* ctx, void** stream);

@@ -78,6 +78,11 @@ int oracle_phys_run(const astro_params* p, PositionMass* pm, VelocityRadius* vr,
                     const uint32_t* sys_sizes, uint32_t nsys, float dt, uint32_t nsteps,
                     uint32_t split_passes, double* pos64, oracle_outputs* out);
 
+/* lightingPass (BarnesHut.metal:103-167) in place on ct: planets (type 1) and
+ * dust (type 2) take the light of the first min(num_stars, 5) particles,
+ * whose positions and colours are read before any colour is written. */
+void oracle_lighting(const PositionMass* pm, ColorType* ct, uint32_t n, uint32_t num_stars);
+
 /* FP64 softened direct sum for sampled particles against their own system. */
 void oracle_direct_accel_f64(const PositionMass* pm, const double* pos64, uint32_t n,
                              const uint32_t* sys_sizes, uint32_t nsys,

@@ -78,6 +78,8 @@ def lib() -> ctypes.CDLL:
         l.oracle_direct_accel_f64.restype = None
         l.oracle_direct_accel_f64.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32,
                                               c_void_p, c_uint32, c_double, c_double, c_void_p]
+        l.oracle_lighting.restype = None
+        l.oracle_lighting.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32]
         _lib = l
     return _lib
 
@@ -183,4 +185,12 @@ def direct_accel(pm, samples, g=1.0, eps=0.01, sizes=None, pos64=None) -> np.nda
     sz = None if sizes is None else np.ascontiguousarray(sizes, np.uint32)
     lib().oracle_direct_accel_f64(_p(pm), _p(pos64), len(pm), _p(sz), 0 if sz is None else len(sz),
                                   _p(s), len(s), g, eps, _p(out))
+    return out
+
+
+def lighting(pm, ct, num_stars=5):
+    """lightingPass on a copy of ct (ColorType[]); returns the new colours."""
+    pm = np.ascontiguousarray(pm)
+    out = np.array(ct, copy=True)
+    lib().oracle_lighting(_p(pm), _p(out), len(pm), num_stars)
     return out

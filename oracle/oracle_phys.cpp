@@ -325,7 +325,7 @@ struct PhysState {
     static constexpr uint32_t kFlagDelta = 0x8u;      // ASTRO_FLAG_OPEN_DELTA
     static constexpr uint32_t kFlagQuad = 0x10u;      // ASTRO_FLAG_QUADRUPOLE
     static constexpr uint32_t kFlagPerParticle = 0x20u;  // ASTRO_FLAG_PER_PARTICLE
-    static constexpr uint32_t kGroup = 32;            // particles per group walk
+    static constexpr uint32_t kGroupMax = 32;         // largest group (one warp)
 
     // One accumulator (plain or Kahan) per component.
     struct Acc {
@@ -469,12 +469,14 @@ struct PhysState {
     }
 
     // Groups for the group walk: every particle in exactly one group of at
-    // most kGroup consecutive (sorted) particles of one system.
+    // most kGroup consecutive (sorted) particles of one system, kGroup =
+    // params.group_size (0 = 32).
     //  - a node with more than kGroup particles packs its consecutive small
     //    children (at most kGroup particles each) greedily, in child order;
     //  - a top-layer node with at most kGroup particles is a group;
     //  - a leaf with more than kGroup particles is cut into kGroup chunks.
     std::vector<std::pair<uint32_t, uint32_t>> make_groups() const {
+        const uint32_t kGroup = p.group_size ? p.group_size : kGroupMax;
         std::vector<std::pair<uint32_t, uint32_t>> groups;
         for (uint32_t l = 0; l < layers; ++l)
             for (uint32_t k = 0; k < counts[l]; ++k) {

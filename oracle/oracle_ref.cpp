@@ -203,6 +203,39 @@ uint64_t oracle_layer_layout(uint32_t count, uint32_t nsys, uint32_t lbits, uint
     return off;
 }
 
+// lightingPass (BarnesHut.metal:103-167): for s < min(numStars, 5) (the
+// unrolled "if (numStars >= s+1)" blocks), in order:
+//   dist = length(x_s - x); d = max(dist / LIGHT_ATTENUATION_DISTANCE, 1e-9)
+//   (bridge.h:98: 4e5); light += rgb_s * (1 / (d * d));
+// rgb = light; alpha = type 2 ? min(max(r, max(g, b)), 0.25) : 1 (:161-166).
+// The lights are read first: no colour written here feeds another particle.
+void oracle_lighting(const PositionMass* pm, ColorType* ct, uint32_t n, uint32_t num_stars) {
+    const uint32_t nl = std::min(std::min(num_stars, 5u), n);
+    float lp[5][3], lc[5][3];
+    for (uint32_t s = 0; s < nl; ++s)
+        for (int a = 0; a < 3; ++a) {
+            lp[s][a] = pm[s].position[a];
+            lc[s][a] = ct[s].color[a];
+        }
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t type = ct[i].type;
+        if (type != 1u && type != 2u) continue;
+        float light[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t s = 0; s < nl; ++s) {
+            const float dx = lp[s][0] - pm[i].position[0];
+            const float dy = lp[s][1] - pm[i].position[1];
+            const float dz = lp[s][2] - pm[i].position[2];
+            const float dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+            const float d = std::max(dist / 4e5f, 1e-9f);
+            const float att = 1.0f / (d * d);
+            for (int a = 0; a < 3; ++a) light[a] = light[a] + lc[s][a] * att;
+        }
+        for (int a = 0; a < 3; ++a) ct[i].color[a] = light[a];
+        ct[i].color[3] = type == 2u ? std::min(std::max(light[0], std::max(light[1], light[2])), 0.25f)
+                                    : 1.0f;
+    }
+}
+
 }  // extern "C"
 
 namespace {

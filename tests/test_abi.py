@@ -54,6 +54,13 @@ _Static_assert(offsetof(OctreeNode, emittedColor) == 48, "ec");
 _Static_assert(offsetof(OctreeNode, emittedColorCenter) == 64, "ecc");
 _Static_assert(offsetof(OctreeNode, children) == 80, "children");
 _Static_assert(offsetof(OctreeNode, layer) == 112, "layer");
+_Static_assert(offsetof(astro_params, block_warps) == 60, "block_warps");
+_Static_assert(offsetof(astro_params, group_size) == 64, "group_size");
+_Static_assert(offsetof(astro_params, sort_variant) == 68, "sort_variant");
+_Static_assert(sizeof(astro_params) == 88, "astro_params");
+_Static_assert(sizeof(astro_state_header) == 136, "astro_state_header");
+_Static_assert(offsetof(astro_state_header, params) == 16, "state params");
+_Static_assert(offsetof(astro_state_header, n) == 120, "state n");
 int main(void) {{ return 0; }}
 """)
     res = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-c", str(src), "-o",
@@ -64,7 +71,29 @@ int main(void) {{ return 0; }}
 def test_python_layouts_match_header():
     from astro_gb300 import layouts as L
 
-    assert ctypes.sizeof(L.Params) == 4 * 4 + 4 * 7 + 4 * 3 + 4 * 2 + 4 * 6
+    assert ctypes.sizeof(L.Params) == 4 * 4 + 4 * 7 + 4 * 3 + 4 * 2 + 4 * 6 == 88
+    assert L.Params.group_size.offset == 64 and L.Params.sort_variant.offset == 68
+    assert ctypes.sizeof(L.StateHeader) == 136 and L.StateHeader.n.offset == 120
+
+
+def test_load_state_rejects_bad_files_without_device(native, tmp_path):
+    from astro_gb300 import layouts as L
+    from astro_gb300._native import lib
+
+    h = c_void_p()
+    missing = str(tmp_path / "absent.state").encode()
+    assert lib().astro_load_state(missing, 0, byref(h), None, None) == -1
+    bad = tmp_path / "bad.state"
+    bad.write_bytes(b"NOTSTATE" + bytes(200))
+    assert lib().astro_load_state(str(bad).encode(), 0, byref(h), None, None) == -1
+    # A valid header whose arrays are cut short.
+    hdr = L.StateHeader(magic=L.STATE_MAGIC, version=L.STATE_VERSION,
+                        header_bytes=ctypes.sizeof(L.StateHeader), n=10, n_tree=10, nsys=1)
+    lib().astro_params_default(L.PRESET_PHYSICAL, byref(hdr.params))
+    short = tmp_path / "short.state"
+    short.write_bytes(bytes(hdr) + bytes(64))
+    assert lib().astro_load_state(str(short).encode(), 0, byref(h), None, None) == -1
+    assert not h.value
     assert L.OCTREE_NODE.itemsize == 128 and L.POSITION_MASS.itemsize == 32
 
 
@@ -80,8 +109,9 @@ def test_params_defaults(native):
         6, pytest.approx(0.7), pytest.approx(1e11), pytest.approx(0.01), 50.0, 1e5)
     assert p.quant_offset == 1e6 and p.damping == pytest.approx(0.9995)
     assert list(p.type_accel_scale) == [5.0, 5.0, 1.0]
+    assert p.light_sources == 5  # numStars (Renderer.swift:26)
     assert lib().astro_params_default(L.PRESET_PHYSICAL, byref(p)) == 0
-    assert p.g == 1.0 and p.bucket == 16
+    assert p.g == 1.0 and p.bucket == 16 and p.light_sources == 0
     assert lib().astro_params_default(7, byref(p)) == -1
 
 
@@ -95,6 +125,12 @@ def test_argument_errors_without_device(native):
     bad = p.replace(lbits=0)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(theta=-1.0)
+    assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
+    bad = p.replace(group_size=33)
+    assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
+    bad = p.replace(sort_variant=8)
+    assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
+    bad = p.replace(light_sources=5)  # lighting needs the REFERENCE preset
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = L.Params()
     lib().astro_params_default(L.PRESET_REFERENCE, byref(bad))

@@ -191,6 +191,45 @@ def test_physical_fast_within_tolerance(ag, oracle, walk, warps, persistent):
     assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
 
 
+@pytest.mark.parametrize("group_size,sort_variant,form", [(8, 1, 0), (16, 4, 1), (1, 7, 0),
+                                                         (32, 6, 1), (5, 2, 0), (24, 3, 0),
+                                                         (12, 5, 0)])
+def test_group_size_and_sort_variant_bit_exact(ag, oracle, group_size, sort_variant, form):
+    """Particles per warp and the sort's pass kernel are tuning knobs: every
+    setting must give the oracle's tree and accelerations bit for bit."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=10, form=form, group_size=group_size,
+                          sort_variant=sort_variant, flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    pm, vr = ic.plummer(16384, seed=1001)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+@pytest.mark.parametrize("group_size,form", [(4, 0), (12, 0), (16, 1), (7, 1)])
+def test_physical_fast_small_groups_within_tolerance(ag, oracle, group_size, form):
+    """Groups of at most 16 run as several copies that split the source
+    lists; the sum must stay within the fast path's tolerance."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, softening=0.005, lbits=14, group_size=group_size,
+                          form=form)
+    pm, vr = ic.disk_bulge(32768, seed=1002)
+    out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=1)
+    ref = oracle.phys_run(p, pm.copy(), vr.copy(), dt=5e-4, steps=1)
+    assert_tree_equal(out, ref)
+    ok, rel = acc_close(out["acc4"], ref["acc4"])
+    assert ok.all(), f"{(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
+    assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
+
+
 def test_physical_precision_form_bit_exact(ag, oracle):
     from astro_gb300 import ic
 
@@ -383,3 +422,37 @@ def test_large_uniform_cube_properties(ag):
     assert top["totalMass"][0] == pytest.approx(1.0, rel=1e-4)
     err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
     assert np.median(err) < 1e-2
+
+
+# ------------------------------------------------------------- lighting --
+
+def test_lighting_pass_bit_exact(ag, oracle):
+    """lightingPass alone and inside the REFERENCE step (between barnesHut and
+    updateSpheres, so it sees the positions before the kick-drift)."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr, ct = ic.reference_scene(5, 200, 20000, seed=3)
+    n = len(pm)
+    p = ag.default_params(L.PRESET_REFERENCE)
+    with ag.Simulation(p, max_n=n) as sim:
+        sim.upload(pm, vr, ct, n_tree=205)
+        sim.lighting_pass(5)
+        got = sim.read_colors()
+    want = oracle.lighting(pm, ct, 5)
+    assert np.array_equal(got["color"], want["color"])
+    assert np.array_equal(got["type"], ct["type"])
+    lit = want["type"] != 0
+    assert (want["color"][lit] != ct["color"][lit]).any()
+    # In the step: colours from the positions at the start of the step.
+    with ag.Simulation(p, max_n=n) as sim:
+        sim.upload(pm, vr, ct, n_tree=205)
+        sim.draw(1.0 / 60, 1)
+        assert np.array_equal(sim.read_colors()["color"], want["color"])
+        moved, _ = sim.download()
+    assert not np.array_equal(moved["position"], pm["position"])
+    # light_sources = 0 leaves the colours as uploaded.
+    with ag.Simulation(p.replace(light_sources=0), max_n=n) as sim:
+        sim.upload(pm, vr, ct, n_tree=205)
+        sim.draw(1.0 / 60, 1)
+        assert np.array_equal(sim.read_colors()["color"], ct["color"])

@@ -1,0 +1,69 @@
+"""Host-side logic without a GPU: workload definitions, the autotuner's
+search space and result file, and the benchmark's knob resolution."""
+import json
+import sys
+from pathlib import Path
+from types import SimpleNamespace
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_workloads_match_their_descriptions():
+    from astro_gb300.workloads import WORKLOADS
+
+    assert sorted(WORKLOADS) == ["c1", "c2", "c3", "c4", "c5"]
+    assert WORKLOADS["c2"].n == 524288 and WORKLOADS["c5"].n == 1 << 24
+    assert WORKLOADS["c4"].generator == "batch"
+    assert len({w.seed for w in WORKLOADS.values()}) == 5
+
+
+def test_autotune_candidates_stay_in_range():
+    from astro_gb300 import autotune
+
+    for n in (16, 16384, 524288, 1 << 22, 1 << 24):
+        c = autotune.candidates("lbits", n)
+        assert c == sorted(c) and all(3 <= v <= 21 for v in c)
+    assert autotune.candidates("group_size", 1000)[-1] == 32
+    assert set(autotune.candidates("block_warps", 1)) <= {2, 4, 8}
+    assert autotune.candidates("sort_variant", 1) == list(range(1, 8))
+    with pytest.raises(KeyError):
+        autotune.candidates("theta", 1)
+
+
+def test_tuned_file_feeds_bench_knobs(tmp_path, monkeypatch):
+    from astro_gb300 import autotune
+
+    f = tmp_path / "tuned.json"
+    f.write_text(json.dumps({"results": {"c2/plain": {"knobs": {
+        "lbits": 12, "bucket": 32, "group_size": 16, "block_warps": 8, "sort_variant": 3}}}}))
+    monkeypatch.setattr(autotune, "TUNED_PATH", f)
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    args = SimpleNamespace(workload="c2", form="plain", no_tuned=False, lbits=None, bucket=20,
+                           warps=None, group_size=None, sort_variant=None)
+    k, src = bench.knobs(args)
+    assert k == {"lbits": 12, "bucket": 20, "block_warps": 8, "group_size": 16, "sort_variant": 3}
+    assert src["bucket"] == "command line" and src["lbits"] == "autotuner"
+    args.form = "precision"  # no entry: preset defaults
+    k, src = bench.knobs(args)
+    assert k["lbits"] == 14 and k["group_size"] == 0 and src["lbits"] == "default"
+    args.form, args.no_tuned = "plain", True
+    assert bench.knobs(args)[0]["lbits"] == 14
+
+
+def test_autotune_load_without_file(tmp_path, monkeypatch):
+    from astro_gb300 import autotune
+
+    monkeypatch.setattr(autotune, "TUNED_PATH", tmp_path / "absent.json")
+    assert autotune.load() == {}
+
+
+def test_driver_arguments():
+    from astro_gb300 import driver
+
+    a = driver.parse(["--scene", "plummer", "--n", "100", "--steps", "7", "--save-every", "3"])
+    assert (a.scene, a.n, a.steps, a.save_every, a.resume) == ("plummer", 100, 7, 3, None)
+    assert set(driver.SCENES) >= {"reference", "disk_bulge", "uniform_cube"}

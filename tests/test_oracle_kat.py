@@ -205,10 +205,29 @@ def test_group_walk_covers_every_particle_once(oracle, native):
     # interacts with every other exactly once, whatever the group layout.
     from astro_gb300 import ic
 
-    for lbits, n in [(6, 3000), (21, 3000), (3, 500)]:
+    for lbits, n, gsize in [(6, 3000, 0), (21, 3000, 0), (3, 500, 0), (10, 2000, 1),
+                            (10, 2000, 7), (6, 3000, 16)]:
         pm, vr = ic.disk_bulge(n, seed=4)
-        out = oracle.phys_run(phys_params(theta=1e-6, lbits=lbits), pm.copy(), vr.copy(), dt=0.0)
+        p = phys_params(theta=1e-6, lbits=lbits, group_size=gsize)
+        out = oracle.phys_run(p, pm.copy(), vr.copy(), dt=0.0)
         assert out["interactions"] == n * (n - 1)
+
+
+def test_smaller_groups_test_more_nodes(oracle, native):
+    # Smaller groups have tighter boxes: fewer interactions and node tests
+    # per particle (but more walks); the same tree and nearly the same
+    # accelerations.
+    from astro_gb300 import ic
+
+    pm, vr = ic.plummer(8192, seed=1001)
+    runs = {g: oracle.phys_run(phys_params(lbits=14, group_size=g), pm.copy(), vr.copy(), dt=0.0)
+            for g in (8, 32)}
+    assert runs[8]["interactions"] < runs[32]["interactions"]
+    assert runs[8]["node_visits"] < runs[32]["node_visits"]
+    assert np.array_equal(runs[8]["sorted_codes"], runs[32]["sorted_codes"])
+    a8, a32 = runs[8]["acc4"][:, :3], runs[32]["acc4"][:, :3]
+    rel = np.linalg.norm(a8 - a32, axis=1) / np.linalg.norm(a32, axis=1)
+    assert np.median(rel) < 2e-3
 
 
 def test_precision_form_runs_and_tracks_plain(oracle, native):
@@ -221,3 +240,33 @@ def test_precision_form_runs_and_tracks_plain(oracle, native):
     d = np.abs(plain["acc4"] - prec["acc4"]).max() / np.abs(plain["acc4"]).max()
     assert d < 1e-3
     assert prec["pos64"].shape == (4096, 3)
+
+
+def test_lighting_known_answers(oracle):
+    # One star at the origin (rgb 1, 0.5, 0.25); a planet at the attenuation
+    # distance 4e5 gets exactly the star's colour; dust at 8e5 a quarter of it
+    # and alpha min(max channel, 0.25); a second star is left alone.
+    pm, _ = particles([[0, 0, 0], [4e5, 0, 0], [0, 8e5, 0], [0, 0, 3e5]])
+    ct = np.zeros(4, L.COLOR_TYPE)
+    ct["type"] = [0, 1, 2, 0]
+    ct["color"][0] = [1.0, 0.5, 0.25, 1.0]
+    ct["color"][3] = [0.1, 0.2, 0.3, 1.0]
+    out = oracle.lighting(pm, ct, num_stars=1)
+    assert out["color"][1].tolist() == [1.0, 0.5, 0.25, 1.0]
+    assert out["color"][2].tolist() == [0.25, 0.125, 0.0625, 0.25]
+    assert out["color"][3].tolist() == pytest.approx([0.1, 0.2, 0.3, 1.0])
+    assert np.array_equal(out["color"][0], ct["color"][0])
+    # The lights are the first num_stars particles, read before the pass: a
+    # planet among them lights with its colour from before (zero here).
+    two = oracle.lighting(pm, ct, num_stars=2)
+    assert two["color"][2].tolist() == [0.25, 0.125, 0.0625, 0.25]
+    ct_b = ct.copy()
+    ct_b["color"][1] = [0.5, 0.5, 0.5, 1.0]
+    three = oracle.lighting(pm, ct_b, num_stars=2)
+    assert three["color"][2][0] == pytest.approx(0.25 + 0.5 / (np.hypot(4e5, 8e5) / 4e5) ** 2)
+    # A planet on top of a light saturates at 1 / (1e-9)^2.
+    pm2, _ = particles([[0, 0, 0], [0, 0, 0]])
+    ct2 = np.zeros(2, L.COLOR_TYPE)
+    ct2["type"] = [0, 1]
+    ct2["color"][0] = [1.0, 0, 0, 1]
+    assert oracle.lighting(pm2, ct2, 1)["color"][1][0] == np.float32(1.0 / np.float32(1e-9) ** 2)
