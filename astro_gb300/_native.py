@@ -61,6 +61,7 @@ SIGNATURES = {
                                  POINTER(c_uint64)]),
     "astro_direct_accel_f64": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "astro_lighting": (c_int, [c_void_p, c_uint32]),
+    "astro_splat": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
     "astro_read_colors": (c_int, [c_void_p, c_void_p, c_uint32]),
     "astro_save_state": (c_int, [c_void_p, c_char_p, c_uint64, c_double]),
     "astro_load_state": (c_int, [c_char_p, c_uint32, POINTER(c_void_p), POINTER(c_uint64),

@@ -21,7 +21,8 @@ OBJ_DIR = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-SOURCES = ["sort.cu", "sort_noalloc.cu", "build.cu", "traverse.cu", "context.cu", "ic.cpp"]
+SOURCES = ["sort.cu", "sort_noalloc.cu", "build.cu", "traverse.cu", "splat.cu", "context.cu",
+           "ic.cpp"]
 
 
 def nvcc() -> str:

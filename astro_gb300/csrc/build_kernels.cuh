@@ -159,6 +159,33 @@ cudaError_t launch_colors_out(const float4* colors, const uint32_t* types, Color
 cudaError_t launch_kick_drift(bool prec, float4* pos, float4* vel, double* x64, const float4* acc,
                               uint32_t n, float dt, cudaStream_t st);
 
+// Headless splat (splat.cu).
+struct SplatArgs {
+    const float4* pos;       // REFERENCE state, upload order
+    const float4* vel;       // w = radius
+    const float4* colors;
+    const uint32_t* types;
+    uint32_t n;
+    float view[16];          // column-major
+    float proj[16];          // column-major
+    float cam[3];
+    uint32_t width, height;
+    float clear[4];
+    float clear_depth;
+    float4* prim;            // per particle: window x, y, depth, size / radius (pixels)
+    uint32_t* kind;          // 0 culled, 1 disc, 2 point
+    uint64_t* keys;          // fragments (pixel << 32 | particle)
+    uint32_t cap;
+    uint32_t* cursor;
+    float4* image;           // width * height, row 0 = top
+    float* depth;
+};
+cudaError_t launch_splat_project(const SplatArgs& a, cudaStream_t st);
+cudaError_t launch_splat_emit(const SplatArgs& a, cudaStream_t st);
+cudaError_t launch_splat_clear(const SplatArgs& a, cudaStream_t st);
+cudaError_t launch_splat_fold(const SplatArgs& a, const uint64_t* keys, uint32_t count,
+                              cudaStream_t st);
+
 // Traversal (traverse.cu).
 struct TraverseConfig {
     bool exact;       // correctly rounded arithmetic (reproduces the CPU restatement)

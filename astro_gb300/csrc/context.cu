@@ -559,6 +559,14 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->types);
     dev_free(ctx->colors);
     dev_free(ctx->lights);
+    dev_free(ctx->splat_prim);
+    dev_free(ctx->splat_kind);
+    dev_free(ctx->splat_image);
+    dev_free(ctx->splat_depth);
+    dev_free(ctx->frag_keys);
+    dev_free(ctx->frag_sorted);
+    dev_free(ctx->frag_vals);
+    if (ctx->frag_temp) cudaFree(ctx->frag_temp);
     dev_free(ctx->codes);
     dev_free(ctx->sorted_keys);
     dev_free(ctx->perm);
@@ -973,6 +981,85 @@ int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n) {
     ColorType* tmp = static_cast<ColorType*>(ctx->staging);
     CK(astro::launch_colors_out(ctx->colors, ctx->types, tmp, n, ctx->stream));
     CK(cudaMemcpyAsync(ct, tmp, sizeof(ColorType) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_device(ctx);
+}
+
+int astro_splat(astro_ctx* ctx, const astro_camera* camera, uint32_t width, uint32_t height,
+                const float* clear, float* rgba, float* depth) {
+    NEED_UPLOAD();
+    if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "the splat draws the REFERENCE preset");
+    if (!camera || !rgba || width == 0 || height == 0)
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "splat: bad camera, image or size");
+    const uint64_t pixels = (uint64_t)width * height;
+    if (pixels > (1ull << 31)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "splat: image too large");
+    cudaStream_t st = ctx->stream;
+    if (!ctx->splat_prim) {
+        CK(dev_alloc(&ctx->splat_prim, ctx->max_n));
+        CK(dev_alloc(&ctx->splat_kind, ctx->max_n + 1));  // + the fragment cursor
+    }
+    if (pixels > ctx->splat_pixels) {
+        dev_free(ctx->splat_image);
+        dev_free(ctx->splat_depth);
+        ctx->splat_pixels = 0;
+        CK(dev_alloc(&ctx->splat_image, pixels));
+        CK(dev_alloc(&ctx->splat_depth, pixels));
+        ctx->splat_pixels = pixels;
+    }
+    astro::SplatArgs a{};
+    a.pos = ctx->pos[0];
+    a.vel = ctx->vel[0];
+    a.colors = ctx->colors;
+    a.types = ctx->types;
+    a.n = ctx->n;
+    std::memcpy(a.view, camera->view, sizeof(a.view));
+    std::memcpy(a.proj, camera->projection, sizeof(a.proj));
+    std::memcpy(a.cam, camera->position, sizeof(a.cam));
+    a.width = width;
+    a.height = height;
+    const float background[4] = {0.0f / 255.0f, 0.0f / 255.0f, 1.0f / 255.0f, 1.0f};  // Renderer.swift:46
+    std::memcpy(a.clear, clear ? clear : background, sizeof(a.clear));
+    a.clear_depth = 1.0f;  // Renderer.swift:768
+    a.prim = ctx->splat_prim;
+    a.kind = ctx->splat_kind;
+    a.cursor = ctx->splat_kind + ctx->max_n;
+    a.image = ctx->splat_image;
+    a.depth = ctx->splat_depth;
+    CK(astro::launch_splat_project(a, st));
+    // Fragments: emit, and emit again into a larger buffer if they overflowed.
+    uint32_t count = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        a.keys = ctx->frag_keys;
+        a.cap = ctx->frag_cap;
+        CK(cudaMemsetAsync(a.cursor, 0, sizeof(uint32_t), st));
+        CK(astro::launch_splat_emit(a, st));
+        CK(cudaMemcpyAsync(&count, a.cursor, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (count <= ctx->frag_cap) break;
+        dev_free(ctx->frag_keys);
+        dev_free(ctx->frag_sorted);
+        dev_free(ctx->frag_vals);
+        if (ctx->frag_temp) cudaFree(ctx->frag_temp);
+        ctx->frag_temp = nullptr;
+        ctx->frag_cap = 0;
+        const uint32_t cap = (uint32_t)std::min<uint64_t>((uint64_t)count + count / 4 + 1024, 0xFFFFFFFFull);
+        const uint32_t key_bits = 64;
+        ctx->frag_temp_bytes = astro::sort_plan(cap, key_bits).total;
+        CK(dev_alloc(&ctx->frag_keys, cap));
+        CK(dev_alloc(&ctx->frag_sorted, cap));
+        CK(dev_alloc(&ctx->frag_vals, cap));
+        CK(cudaMalloc(&ctx->frag_temp, ctx->frag_temp_bytes));
+        ctx->frag_cap = cap;
+    }
+    if (count > ctx->frag_cap) return fail(ctx, ASTRO_ERR_CAPACITY, "splat: fragment count grew");
+    // Sort by (pixel, particle): the per-pixel draw order.
+    uint32_t pixel_bits = 0;
+    while ((1ull << pixel_bits) < pixels) ++pixel_bits;
+    CK(astro::sort_pairs(ctx->frag_keys, nullptr, ctx->frag_sorted, ctx->frag_vals, count, nullptr,
+                         32u + pixel_bits, ctx->frag_temp, ctx->frag_temp_bytes, st, ctx->err));
+    CK(astro::launch_splat_clear(a, st));
+    CK(astro::launch_splat_fold(a, ctx->frag_sorted, count, st));
+    CK(cudaMemcpyAsync(rgba, ctx->splat_image, 16ull * pixels, cudaMemcpyDeviceToHost, st));
+    if (depth) CK(cudaMemcpyAsync(depth, ctx->splat_depth, 4ull * pixels, cudaMemcpyDeviceToHost, st));
     return check_device(ctx);
 }
 

@@ -92,6 +92,18 @@ struct astro_ctx {
     float4* acc = nullptr;
     float4* colors = nullptr;         // REFERENCE: ColorType colours (lighting pass)
     float4* lights = nullptr;         // REFERENCE: lighting pass light snapshot
+    // Headless splat (allocated on first use).
+    float4* splat_prim = nullptr;
+    uint32_t* splat_kind = nullptr;
+    float4* splat_image = nullptr;
+    float* splat_depth = nullptr;
+    uint64_t splat_pixels = 0;
+    uint64_t* frag_keys = nullptr;
+    uint64_t* frag_sorted = nullptr;
+    uint32_t* frag_vals = nullptr;
+    void* frag_temp = nullptr;
+    size_t frag_temp_bytes = 0;
+    uint32_t frag_cap = 0;
     uint32_t* types = nullptr;
     uint64_t* codes = nullptr;        // keys in the state order before sorting
     uint64_t* sorted_keys = nullptr;

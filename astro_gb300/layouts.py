@@ -149,3 +149,14 @@ def read_state(path):
     if off != len(raw):
         raise ValueError("state file size does not match its header")
     return h, sizes, pm, vr, ids, types, pos64
+
+
+class CameraABI(ctypes.Structure):
+    """astro_camera: column-major view and projection matrices, camera position."""
+
+    _fields_ = [
+        ("view", ctypes.c_float * 16),
+        ("projection", ctypes.c_float * 16),
+        ("position", ctypes.c_float * 3),
+        ("_pad", ctypes.c_float),
+    ]

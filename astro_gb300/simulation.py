@@ -142,6 +142,18 @@ class Simulation:
         self._check(lib().astro_read_colors(self._h, ptr(ct), self.n))
         return ct
 
+    def splat(self, camera, width: int, height: int, clear=None):
+        """Headless scene pass (astro_splat): (rgba[h, w, 4], depth[h, w])."""
+        from .render import to_abi
+
+        cam = to_abi(camera)
+        rgba = np.zeros((height, width, 4), np.float32)
+        depth = np.zeros((height, width), np.float32)
+        cl = None if clear is None else np.ascontiguousarray(clear, np.float32)
+        self._check(lib().astro_splat(self._h, byref(cam), width, height, ptr(cl), ptr(rgba),
+                                      ptr(depth)))
+        return rgba, depth
+
     def draw(self, dt: float, steps: int = 1) -> None:
         """Run `steps` full steps (graph-replayed unless FLAG_NO_GRAPH)."""
         self._check(lib().astro_step(self._h, dt, steps))

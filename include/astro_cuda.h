@@ -273,6 +273,29 @@ int astro_lighting(astro_ctx* ctx, uint32_t num_stars);
 int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n);
 
 /* ---------------------------------------------------------------------------
+ * Headless splat: the scene pass of the reference's renderer
+ * (Spheres.metal:23-64, Renderer.swift:780-830) into an image, REFERENCE
+ * preset. Each particle is projected as clip = P * (V * (x - camera, 1)).
+ * Stars and planets (types 0, 1) are drawn as opaque discs of their sphere's
+ * projected radius (the unit-extent sphere mesh scaled by the radius) at the
+ * centre's depth; dust (type 2) as blended point sprites of `radius` pixels.
+ * Draw order is particle order, the depth test is "less" with depth writes,
+ * and every colour write is rounded to half precision (rgba16Float).
+ * ------------------------------------------------------------------------- */
+typedef struct astro_camera {
+    float view[16];           /* column-major (simd_float4x4 columns): viewMatrix */
+    float projection[16];     /* column-major: projectionMatrix */
+    float position[3];        /* cameraPosition */
+    float _pad;
+} astro_camera;
+
+/* rgba: width * height * 4 floats, row 0 at the top; depth: width * height
+ * floats or NULL (host buffers). clear: RGBA clear colour, NULL for the
+ * reference's background (0, 0, 1/255, 1); depth clears to 1. */
+int astro_splat(astro_ctx* ctx, const astro_camera* camera, uint32_t width, uint32_t height,
+                const float* clear, float* rgba, float* depth);
+
+/* ---------------------------------------------------------------------------
  * State files: the role of makeSpheres / resetSimulation
  * (Renderer.swift:148-152,441-493) for a headless step loop, which the
  * reference rebuilds from an unseeded generator on every reset.

@@ -83,6 +83,12 @@ int oracle_phys_run(const astro_params* p, PositionMass* pm, VelocityRadius* vr,
  * whose positions and colours are read before any colour is written. */
 void oracle_lighting(const PositionMass* pm, ColorType* ct, uint32_t n, uint32_t num_stars);
 
+/* Headless splat (astro_splat's definition) drawn sequentially: rgba
+ * (width * height * 4) and depth (width * height) receive the image. */
+void oracle_splat(const PositionMass* pm, const VelocityRadius* vr, const ColorType* ct, uint32_t n,
+                  const float* view, const float* proj, const float* cam, uint32_t width,
+                  uint32_t height, const float* clear, float* rgba, float* depth);
+
 /* FP64 softened direct sum for sampled particles against their own system. */
 void oracle_direct_accel_f64(const PositionMass* pm, const double* pos64, uint32_t n,
                              const uint32_t* sys_sizes, uint32_t nsys,

@@ -78,6 +78,9 @@ def lib() -> ctypes.CDLL:
         l.oracle_direct_accel_f64.restype = None
         l.oracle_direct_accel_f64.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32,
                                               c_void_p, c_uint32, c_double, c_double, c_void_p]
+        l.oracle_splat.restype = None
+        l.oracle_splat.argtypes = [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
+                                   c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]
         l.oracle_lighting.restype = None
         l.oracle_lighting.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32]
         _lib = l
@@ -194,3 +197,19 @@ def lighting(pm, ct, num_stars=5):
     out = np.array(ct, copy=True)
     lib().oracle_lighting(_p(pm), _p(out), len(pm), num_stars)
     return out
+
+
+def splat(pm, vr, ct, camera, width, height, clear=(0.0, 0.0, 1.0 / 255.0, 1.0)):
+    """The headless splat drawn sequentially: (rgba[h, w, 4], depth[h, w]).
+    camera: astro_gb300.render.Camera (view, projection, position)."""
+    n = len(pm)
+    view = np.ascontiguousarray(camera.view, np.float32).reshape(16)
+    proj = np.ascontiguousarray(camera.projection, np.float32).reshape(16)
+    pos = np.ascontiguousarray(camera.position, np.float32).reshape(3)
+    cl = np.ascontiguousarray(clear, np.float32)
+    rgba = np.zeros((height, width, 4), np.float32)
+    depth = np.zeros((height, width), np.float32)
+    lib().oracle_splat(_p(np.ascontiguousarray(pm)), _p(np.ascontiguousarray(vr)),
+                       _p(np.ascontiguousarray(ct)), n, _p(view), _p(proj), _p(pos), width, height,
+                       _p(cl), _p(rgba), _p(depth))
+    return rgba, depth

@@ -456,3 +456,32 @@ def test_lighting_pass_bit_exact(ag, oracle):
         sim.upload(pm, vr, ct, n_tree=205)
         sim.draw(1.0 / 60, 1)
         assert np.array_equal(sim.read_colors()["color"], ct["color"])
+
+
+# ---------------------------------------------------------------- splat --
+
+@pytest.mark.parametrize("width,height,pos", [(320, 240, (0.0, 0.0, 1.8e6)),
+                                              (257, 131, (2e5, -1e5, 6e5))])
+def test_splat_bit_exact(ag, oracle, width, height, pos):
+    """The headless scene pass against its sequential CPU restatement: every
+    pixel's colour and depth, after the lighting pass, for the reference's
+    camera and a close one (large discs, partly off-screen)."""
+    from astro_gb300 import ic
+    from astro_gb300.render import reference_camera
+
+    L = ag.layouts
+    pm, vr, ct = ic.reference_scene(5, 200, 30000, seed=11)
+    n = len(pm)
+    cam = reference_camera(width, height, position=pos)
+    with ag.Simulation(ag.default_params(L.PRESET_REFERENCE), max_n=n) as sim:
+        sim.upload(pm, vr, ct, n_tree=205)
+        sim.lighting_pass(5)
+        lit = sim.read_colors()
+        rgba, depth = sim.splat(cam, width, height)
+        # A second call reuses the fragment buffers.
+        rgba2, depth2 = sim.splat(cam, width, height)
+    want_rgba, want_depth = oracle.splat(pm, vr, lit, cam, width, height)
+    assert np.array_equal(depth, want_depth)
+    assert np.array_equal(rgba, want_rgba)
+    assert np.array_equal(rgba2, rgba) and np.array_equal(depth2, depth)
+    assert (depth < 1.0).sum() > 100

@@ -270,3 +270,75 @@ def test_lighting_known_answers(oracle):
     ct2["type"] = [0, 1]
     ct2["color"][0] = [1.0, 0, 0, 1]
     assert oracle.lighting(pm2, ct2, 1)["color"][1][0] == np.float32(1.0 / np.float32(1e-9) ** 2)
+
+
+def _flat_camera():
+    # view = identity, projection = identity: clip = (x - cam, 1), so window
+    # coordinates follow directly from the positions.
+    from astro_gb300.render import Camera
+
+    eye = np.eye(4, dtype=np.float32).reshape(16)
+    return Camera(eye.copy(), eye.copy(), np.zeros(3, np.float32))
+
+
+def test_splat_half_rounding_matches_ieee_binary16(oracle):
+    # A one-pixel image whose only fragment is an opaque disc of colour x
+    # returns round_to_half(x): compare with numpy's float16 conversion.
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.normal(0, 1, 200), rng.normal(0, 1e4, 50), [6.1e-5, 5.9e-8, 65519.0,
+                         65520.0, 0.1, 1 / 255]]).astype(np.float32)
+    pm, vr = particles([[0.0, 0.0, 0.5]])
+    vr["radius"] = 4.0
+    ct = np.zeros(1, L.COLOR_TYPE)
+    ct["type"] = 0
+    for x in xs:
+        ct["color"][0] = [x, -x, x / 3, 1.0]
+        rgba, _ = oracle.splat(pm, vr, ct, _flat_camera(), 1, 1)
+        with np.errstate(over="ignore"):
+            want = np.array([x, -x, np.float32(x) / np.float32(3)], np.float32).astype(np.float16)
+        assert np.array_equal(rgba[0, 0, :3], want.astype(np.float32)), x
+
+
+def test_splat_points_discs_depth_and_blending(oracle):
+    from astro_gb300.render import Camera
+
+    cam = _flat_camera()
+    W = H = 8
+    # A dust point of size 2 at the image centre covers the 2 x 2 pixels
+    # around it and blends over the clear colour.
+    pm, vr = particles([[0.0, 0.0, 0.5]])
+    vr["radius"] = 2.0
+    ct = np.zeros(1, L.COLOR_TYPE)
+    ct["type"] = 2
+    ct["color"][0] = [1.0, 0.5, 0.25, 0.25]
+    clear = np.array([0.0, 0.0, 1.0 / 255.0, 1.0], np.float32)
+    rgba, depth = oracle.splat(pm, vr, ct, cam, W, H, clear)
+    hit = depth < 1.0
+    assert hit.sum() == 4 and hit[3:5, 3:5].all()
+    c16 = clear.astype(np.float16).astype(np.float32)
+    a = np.float32(0.25)
+    want_r = np.float16(np.float32(1.0) * a + c16[0] * (np.float32(1) - a)).astype(np.float32)
+    want_b = np.float16(np.float32(0.25) * a + c16[2] * (np.float32(1) - a)).astype(np.float32)
+    assert rgba[3, 3, 0] == want_r and rgba[3, 3, 2] == want_b
+    assert np.array_equal(rgba[0, 0], c16) and depth[0, 0] == 1.0
+    # Two opaque discs: the nearer one wins whatever the draw order; a disc
+    # of radius r (world r/2, H/2 pixels per unit) covers centres within r px.
+    pm, vr = particles([[0.0, 0.0, 0.8], [0.0, 0.0, 0.3]])
+    vr["radius"] = [1.0, 0.5]      # discs of 2 px and 1 px: (radius / 2) * (H / 2)
+    ct = np.zeros(2, L.COLOR_TYPE)
+    ct["type"] = [0, 1]
+    ct["color"] = [[1, 0, 0, 1], [0, 1, 0, 1]]
+    rgba, depth = oracle.splat(pm, vr, ct, cam, W, H)
+    near = depth == np.float32(0.3)
+    far = depth == np.float32(0.8)
+    # The 2 px disc covers the 12 centres within distance 2 of (4, 4); the
+    # 1 px disc in front of it covers the middle 4.
+    assert near.sum() == 4 and far.sum() == 8
+    assert (rgba[near][:, 1] == 1.0).all() and (rgba[far][:, 0] == 1.0).all()
+    rev = oracle.splat(pm[::-1].copy(), vr[::-1].copy(), ct[::-1].copy(), cam, W, H)
+    assert np.array_equal(rev[0], rgba) and np.array_equal(rev[1], depth)
+    # Behind the camera (w <= 0) or beyond the far plane nothing is drawn.
+    pm, vr = particles([[0.0, 0.0, 1.5]])
+    vr["radius"] = 2.0
+    rgba, depth = oracle.splat(pm, vr, ct[:1], cam, W, H)
+    assert (depth == 1.0).all()
