@@ -45,6 +45,10 @@ UNIT = "particle-updates/s"
 FLOPS_PER_INTERACTION = 20
 FLOPS_PER_QUAD_CELL = 50
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one traversal
+# launch, captured with ncu on GB300 for (workload, form, walk) at the tuned
+# knobs: the roofline's "traffic".
+NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 31.9e6}
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -435,22 +439,29 @@ def run_ours(args, world, rank, local):
             sims.append(s1)
         for s1 in sims:
             s1.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # Each system's step waits for the previous one (an event chain
+        # across the contexts' streams), so the systems run one at a time on
+        # the device, as separate launches, without host synchronisation.
+        streams = [torch.cuda.ExternalStream(s1.stream) for s1 in sims]
         torch.cuda.synchronize()
         k1 = max(1, args.steps // 4)
-        e0.record()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(streams[0])
+        prev = e0
         for _ in range(k1):
-            for s1 in sims:
+            for s1, st1 in zip(sims, streams):
+                st1.wait_event(prev)
                 s1.draw(dt, 1)
-        for s1 in sims:
-            s1.synchronize()
-        e1.record()
+                prev = torch.cuda.Event()
+                prev.record(st1)
+        streams[0].wait_event(prev)
+        e1.record(streams[0])
         torch.cuda.synchronize()
         t1 = e0.elapsed_time(e1)
         one_at_a_time = {"value": n * k1 / (t1 * 1e-3), "unit": UNIT, "steps": k1,
                          "ms_per_step": t1 / k1,
                          "how": "plain FP32, one context and step graph per system, "
-                                "stepped in sequence"}
+                                "each system's step waiting for the previous one"}
         for s1 in sims:
             s1.close()
 
@@ -569,7 +580,9 @@ def main():
                                     else "traverse_phys_kernel"),
                          "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
-                         "frac": r["achieved"] / r["fp32_peak"], "traffic": None,
+                         "frac": r["achieved"] / r["fp32_peak"],
+                         "traffic": NCU_TRAVERSAL_DRAM_BYTES.get((args.workload, args.form,
+                                                                   args.walk)),
                          "flops_per_launch": r["flops"],
                          "interactions_per_s": r["interactions"] / (r["trav_ms"] * 1e-3),
                          "launch_ms": r["trav_ms"],
