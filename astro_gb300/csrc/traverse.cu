@@ -402,6 +402,20 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
 // sum, leaf particles (32 at a time through shared memory) into another.
 constexpr int kCellCap = 64;
 constexpr int kLeafCap = 32;
+
+// A staged accepted cell: centre of mass and mass, and with quadrupoles
+// {Qxx, Qyy, Qxy, Qxz} and {Qyz, Qzz}; one record, so the evaluation loop
+// walks a single shared-memory array.
+template <bool kQuad>
+struct CellSlot {
+    float4 cm;
+    float4 q;
+    float4 q2;
+};
+template <>
+struct CellSlot<false> {
+    float4 cm;
+};
 // Resident warps per SM the group walk's register allocation is sized for
 // (0: the compiler's choice).
 #ifndef ASTRO_GROUP_WARPS_PER_SM
@@ -415,9 +429,7 @@ constexpr int kLeafCap = 32;
 
 template <bool kExact, bool kPrec, bool kQuad, int kWarps>
 __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a) {
-    __shared__ float4 s_cm[kWarps][kCellCap];
-    __shared__ float4 s_q[kWarps][kQuad ? kCellCap : 1];   // Qxx, Qyy, Qxy, Qxz
-    __shared__ float2 s_q2[kWarps][kQuad ? kCellCap : 1];  // Qyz, Qzz
+    __shared__ CellSlot<kQuad> s_cell[kWarps][kCellCap];
     __shared__ uint2 s_leaf[kWarps][kLeafCap];
     __shared__ float4 s_tile[kWarps][32];
     __shared__ uint32_t s_jdx[kWarps][32];
@@ -473,15 +485,16 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             if (valid) {
                 if (kExact) {
                     for (uint32_t e = 0; e < n_cell; ++e) {
-                        const float4 c = s_cm[warp][e];
+                        const CellSlot<kQuad>& cs = s_cell[warp][e];
+                        const float4 c = cs.cm;
                         const float dx = __fsub_rn(c.x, me.x), dy = __fsub_rn(c.y, me.y),
                                     dz = __fsub_rn(c.z, me.z);
                         const float r2t = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
                                                     __fmul_rn(dz, dz));
                         float tx, ty, tz;
-                        if (kQuad)
-                            cell_term<true>(dx, dy, dz, r2t, c.w, true, s_q[warp][e], s_q2[warp][e].x,
-                                            g, eps2, tx, ty, tz);
+                        if constexpr (kQuad)
+                            cell_term<true>(dx, dy, dz, r2t, c.w, true, cs.q, cs.q2.x, g, eps2, tx, ty,
+                                            tz);
                         else
                             cell_term<true>(dx, dy, dz, r2t, c.w, false,
                                             make_float4(0.f, 0.f, 0.f, 0.f), 0.f, g, eps2, tx, ty, tz);
@@ -495,17 +508,16 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                     float& rx = kPrec ? px : cells.ax;
                     float& ry = kPrec ? py : cells.ay;
                     float& rz = kPrec ? pz : cells.az;
-#pragma unroll 2
-                    for (uint32_t e = rep; e < n_cell; e += reps) {
-                        const float4 c = s_cm[warp][e];
+                    auto cell = [&](const CellSlot<kQuad>& cs) {
+                        const float4 c = cs.cm;
                         const float dx = c.x - me.x, dy = c.y - me.y, dz = c.z - me.z;
                         const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
                         const float u = inv * inv, inv3 = u * inv;
                         float ex, ey, ez;
-                        if (kQuad) {
+                        if constexpr (kQuad) {
                             // inv^3 [(M + 5/2 u^2 d.Qd) d - u Qd], u = 1/r^2.
-                            const float4 q = s_q[warp][e];
-                            const float2 q2 = s_q2[warp][e];
+                            const float4 q = cs.q;
+                            const float4 q2 = cs.q2;
                             const float qx = fmaf(q.x, dx, fmaf(q.z, dy, q.w * dz));
                             const float qy = fmaf(q.z, dx, fmaf(q.y, dy, q2.x * dz));
                             const float qz = fmaf(q.w, dx, fmaf(q2.x, dy, q2.y * dz));
@@ -522,6 +534,13 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                         rx = fmaf(inv3, ex, rx);
                         ry = fmaf(inv3, ey, ry);
                         rz = fmaf(inv3, ez, rz);
+                    };
+                    if (reps == 1) {
+#pragma unroll 4
+                        for (uint32_t e = 0; e < n_cell; ++e) cell(s_cell[warp][e]);
+                    } else {
+#pragma unroll 2
+                        for (uint32_t e = rep; e < n_cell; e += reps) cell(s_cell[warp][e]);
                     }
                     if (kPrec) cells.add(px, py, pz);
                 }
@@ -580,15 +599,20 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                     float& rz = kPrec ? pz : leaves.az;
                     if (skip_self_free) {
                         // eps > 0: the self term is exactly zero, so no test is needed.
-#pragma unroll 4
-                        for (uint32_t q = rep; q < cnt; q += reps) {
-                            const float4 p = s_tile[warp][q];
+                        auto pp = [&](const float4 p) {
                             const float dx = p.x - me.x, dy = p.y - me.y, dz = p.z - me.z;
                             const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
                             const float sc = p.w * (inv * inv * inv);
                             rx = fmaf(dx, sc, rx);
                             ry = fmaf(dy, sc, ry);
                             rz = fmaf(dz, sc, rz);
+                        };
+                        if (reps == 1) {
+#pragma unroll 4
+                            for (uint32_t q = 0; q < cnt; ++q) pp(s_tile[warp][q]);
+                        } else {
+#pragma unroll 4
+                            for (uint32_t q = rep; q < cnt; q += reps) pp(s_tile[warp][q]);
                         }
                         if (owner) inter += cnt;
                     } else if (kExact) {
@@ -659,11 +683,11 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                     if (n_cell + __popc(bacc) > (uint32_t)kCellCap) flush_cells();
                     if (acc) {
                         const uint32_t slot = n_cell + __popc(bacc & lt);
-                        s_cm[warp][slot] = c;
-                        if (kQuad) {
+                        s_cell[warp][slot].cm = c;
+                        if constexpr (kQuad) {
                             const float4 q = __ldg(&a.node_q[nd]);
-                            s_q[warp][slot] = q;
-                            s_q2[warp][slot] = make_float2(__ldg(&a.node_qyz[nd]), -(q.x + q.y));
+                            s_cell[warp][slot].q = q;
+                            s_cell[warp][slot].q2 = make_float4(__ldg(&a.node_qyz[nd]), -(q.x + q.y), 0.f, 0.f);
                         }
                     }
                     n_cell += __popc(bacc);
