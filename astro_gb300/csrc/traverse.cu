@@ -400,7 +400,9 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
 // (per-warp buffers in global memory). Lists are evaluated by all lanes,
 // one particle per lane, whenever they fill and at the end: cells into one
 // sum, leaf particles (32 at a time through shared memory) into another.
-constexpr int kCellCap = 64;
+// Cell list capacity per warp: the largest that keeps a block's static
+// shared memory under 48 KB.
+constexpr int cell_cap(int warps) { return warps >= 8 ? 96 : 128; }
 constexpr int kLeafCap = 32;
 
 // A staged accepted cell: centre of mass and mass, and with quadrupoles
@@ -429,6 +431,7 @@ struct CellSlot<false> {
 
 template <bool kExact, bool kPrec, bool kQuad, int kWarps>
 __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a) {
+    constexpr int kCellCap = cell_cap(kWarps);
     __shared__ CellSlot<kQuad> s_cell[kWarps][kCellCap];
     __shared__ uint2 s_leaf[kWarps][kLeafCap];
     __shared__ float4 s_tile[kWarps][32];

@@ -73,6 +73,8 @@ def parse():
                     help="the reference's monopole-only cells and size/theta opening test")
     ap.add_argument("--error-samples", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-threads", type=int, default=0,
+                    help="host threads of the CPU restatement (0: all cores)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--one-at-a-time", action="store_true",
@@ -486,7 +488,7 @@ def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
     workload until the time budget is spent (at least one)."""
     from oracle import oracle as orc
 
-    cores = orc.set_threads(0)
+    cores = orc.set_threads(args.cpu_threads)
     steps, t_total = 0, 0.0
     pm_c, vr_c = pm.copy(), vr.copy()
     while True:
@@ -514,7 +516,7 @@ def run_reference(args):
     n = len(pm)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     p, knob_source = make_params(args, ag, L)
-    cores = orc.set_threads(0)
+    cores = orc.set_threads(args.cpu_threads)
     pm_c, vr_c = pm.copy(), vr.copy()
     for _ in range(args.warmup):
         orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
