@@ -348,6 +348,21 @@ __device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint
     return __fmul_rn(crit, crit);
 }
 
+// PHYSICAL centre of mass (and mass) from the raw sums: one correctly rounded
+// reciprocal of the mass and three products (FP64 in the precision form,
+// then rounded to FP32); zero for a massless node.
+__device__ __forceinline__ float4 com_from_sums(float sx, float sy, float sz, float m) {
+    if (!(m > 0.f)) return make_float4(0.f, 0.f, 0.f, m);
+    const float inv = __fdiv_rn(1.0f, m);
+    return make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), m);
+}
+__device__ __forceinline__ float4 com_from_sums(double sx, double sy, double sz, double m) {
+    if (!(m > 0.0)) return make_float4(0.f, 0.f, 0.f, __double2float_rn(m));
+    const double inv = __ddiv_rn(1.0, m);
+    return make_float4(__double2float_rn(__dmul_rn(sx, inv)), __double2float_rn(__dmul_rn(sy, inv)),
+                       __double2float_rn(__dmul_rn(sz, inv)), __double2float_rn(m));
+}
+
 __device__ __forceinline__ void emit_group(const AggArgs& a, uint32_t b, uint32_t e) {
     const uint32_t slot = atomicAdd(a.group_count, 1u);
     a.groups[slot] = make_uint2(b, e);
@@ -391,8 +406,7 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
             sz = __fadd_rn(sz, __fmul_rn(q.w, q.z));
         }
         reinterpret_cast<float4*>(a.node_sum)[j] = make_float4(sx, sy, sz, m);
-        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
-        else cm.w = m;
+        cm = com_from_sums(sx, sy, sz, m);
     } else {
         const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
         const double ox = a.sys[s].origin[0], oy = a.sys[s].origin[1], oz = a.sys[s].origin[2];
@@ -405,10 +419,7 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
             sz = __dadd_rn(sz, __dmul_rn(mi, __dsub_rn(a.x64[2 * (size_t)a.n + i], oz)));
         }
         reinterpret_cast<double4*>(a.node_sum)[j] = make_double4(sx, sy, sz, m);
-        if (m > 0.0)
-            cm = make_float4(__double2float_rn(__ddiv_rn(sx, m)), __double2float_rn(__ddiv_rn(sy, m)),
-                             __double2float_rn(__ddiv_rn(sz, m)), __double2float_rn(m));
-        else cm.w = __double2float_rn(m);
+        cm = com_from_sums(sx, sy, sz, m);
     }
     a.node_cm[j] = cm;
     a.node_rng[j] = make_uint4(0u, 0u, pb, pe);
@@ -490,8 +501,7 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
             }
         }
         reinterpret_cast<float4*>(a.node_sum)[node] = make_float4(sx, sy, sz, m);
-        if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
-        else cm.w = m;
+        cm = com_from_sums(sx, sy, sz, m);
     } else {
         const double4* sum = reinterpret_cast<const double4*>(a.node_sum);
         double4 cs[8];
@@ -508,10 +518,7 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
             }
         }
         reinterpret_cast<double4*>(a.node_sum)[node] = make_double4(sx, sy, sz, m);
-        if (m > 0.0)
-            cm = make_float4(__double2float_rn(__ddiv_rn(sx, m)), __double2float_rn(__ddiv_rn(sy, m)),
-                             __double2float_rn(__ddiv_rn(sz, m)), __double2float_rn(m));
-        else cm.w = __double2float_rn(m);
+        cm = com_from_sums(sx, sy, sz, m);
     }
     a.node_cm[node] = cm;
     a.node_rng[node] = make_uint4(cb, ce, pb, pe);

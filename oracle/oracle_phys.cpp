@@ -284,10 +284,12 @@ struct PhysState {
                     o[1] = sy;
                     o[2] = sz;
                     o[3] = m;
+                    // Centre of mass through one reciprocal of the mass.
                     float* c = &cm[4ull * node];
-                    c[0] = m > 0 ? (float)(sx / m) : 0.0f;
-                    c[1] = m > 0 ? (float)(sy / m) : 0.0f;
-                    c[2] = m > 0 ? (float)(sz / m) : 0.0f;
+                    const double inv = m > 0 ? 1.0 / m : 0.0;
+                    c[0] = m > 0 ? (float)(sx * inv) : 0.0f;
+                    c[1] = m > 0 ? (float)(sy * inv) : 0.0f;
+                    c[2] = m > 0 ? (float)(sz * inv) : 0.0f;
                     c[3] = (float)m;
                 } else {
                     float sx = 0, sy = 0, sz = 0, m = 0;
@@ -313,9 +315,10 @@ struct PhysState {
                     o[2] = sz;
                     o[3] = m;
                     float* c = &cm[4ull * node];
-                    c[0] = m > 0 ? sx / m : 0.0f;
-                    c[1] = m > 0 ? sy / m : 0.0f;
-                    c[2] = m > 0 ? sz / m : 0.0f;
+                    const float inv = m > 0 ? 1.0f / m : 0.0f;
+                    c[0] = m > 0 ? sx * inv : 0.0f;
+                    c[1] = m > 0 ? sy * inv : 0.0f;
+                    c[2] = m > 0 ? sz * inv : 0.0f;
                     c[3] = m;
                 }
             }

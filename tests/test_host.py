@@ -67,3 +67,20 @@ def test_driver_arguments():
     a = driver.parse(["--scene", "plummer", "--n", "100", "--steps", "7", "--save-every", "3"])
     assert (a.scene, a.n, a.steps, a.save_every, a.resume) == ("plummer", 100, 7, 3, None)
     assert set(driver.SCENES) >= {"reference", "disk_bulge", "uniform_cube"}
+
+
+def test_bench_reference_arm_prints_the_contract_line():
+    # The reference arm (CPU restatement) on the small workload: one JSON
+    # line with the metric, the impl tag, the CPU baseline and a zero-copy e2e.
+    import subprocess
+
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--workload", "c1", "--steps", "1", "--warmup", "0", "--cpu-threads", "2"],
+                         capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "particle-updates/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["config"]["workload"].startswith("c1") and line["config"]["n"] == 16384
