@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2",
+                    help="c1..c5: PHYSICAL workloads; ref: the reference's own scene")
     ap.add_argument("--form", choices=["plain", "precision"], default="plain")
     # Launch knobs: unset ones come from the autotuner's file for the
     # workload and form (astro_gb300/tuned.json), else the preset defaults.
@@ -119,6 +120,12 @@ def make_params(args, ag, L):
     w = WORKLOADS[args.workload]
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     k, source = knobs(args)
+    if w.preset == "reference":
+        # The reference's constants; only the tree depth and the sort kernel
+        # apply to its walk.
+        k = {key: k[key] for key in ("lbits", "sort_variant")}
+        source = {key: source[key] for key in k}
+        return ag.default_params(L.PRESET_REFERENCE, theta=args.theta, **k), source
     p = ag.default_params(L.PRESET_PHYSICAL, theta=args.theta, form=form, **k, **w.physics)
     return p.replace(flags=walk_flags(args, L, p.flags)), source
 
@@ -252,6 +259,37 @@ def stage_bytes(n, key_bits, layer_counts, nsys, precision):
     }
 
 
+def sort_alone(torch, n, key_bits, seed, flush, stream, sim, peaks):
+    """astro_radix_sort of n uniform keys of key_bits, after an L2 flush each
+    time: mean of three timed sorts and the HBM roofline figures."""
+    from astro_gb300.radix_sort import RadixSort
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    keys = torch.randint(0, 1 << 62, (n,), device="cuda", generator=g, dtype=torch.int64)
+    if key_bits < 63:
+        keys &= (1 << key_bits) - 1
+    keys_out = torch.empty_like(keys)
+    idx_out = torch.empty(n, dtype=torch.int32, device="cuda")
+    sorter = RadixSort(n, key_bits)
+    sort_ms = []
+    for it in range(4):
+        with torch.cuda.stream(stream):
+            flush.fill_(3)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sorter.sort(keys, None, keys_out, idx_out, n, stream=sim.stream)
+            e1.record(stream)
+        sim.synchronize()
+        if it:
+            sort_ms.append(e0.elapsed_time(e1))
+    passes = (key_bits + 7) // 8
+    sort_b = (8 + 24 * passes - 4) * n
+    ms = float(np.mean(sort_ms))
+    return {"bound": "hbm", "key_bits": key_bits, "passes": passes, "keys": n, "bytes": sort_b,
+            "ms": ms, "achieved": sort_b / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": sort_b / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+
+
 # ---------------------------------------------------------------- ours --
 
 def run_ours(args, world, rank, local):
@@ -269,9 +307,17 @@ def run_ours(args, world, rank, local):
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     p, knob_source = make_params(args, ag, L)
     nsys = len(sizes) if sizes else 1
+    is_ref = w.preset == "reference"
+    ct, n_tree = w.make_colors() if is_ref else (None, n)
     sim = ag.Simulation(p, max_n=n, max_systems=nsys)
-    upload = (lambda: sim.upload_systems(pm, vr, sizes)) if sizes else (lambda: sim.upload(pm, vr))
-    upload()
+
+    def upload_from(pm_, vr_):
+        if sizes:
+            sim.upload_systems(pm_, vr_, sizes)
+        else:
+            sim.upload(pm_, vr_, ct, n_tree=n_tree)
+
+    upload_from(pm, vr)
     stream = torch.cuda.ExternalStream(sim.stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -328,43 +374,22 @@ def run_ours(args, world, rank, local):
     sizes_, offsets, counts = sim.tree_info()
     peaks, peak_src = measured_peaks()
     key_bits = 3 * p.lbits + ((nsys - 1).bit_length() if nsys > 1 else 0)
-    sbytes = stage_bytes(n, key_bits, counts, nsys, form == L.FORM_PRECISION)
-    stage_roofline = {
-        k: {"bytes": int(b), "ms": stages[k], "achieved_gbs": b / (stages[k] * 1e-3) / 1e9,
-            "frac": b / (stages[k] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
-        for k, b in sbytes.items()}
+    stage_roofline = None
+    if not is_ref:
+        sbytes = stage_bytes(n, key_bits, counts, nsys, form == L.FORM_PRECISION)
+        stage_roofline = {
+            k: {"bytes": int(b), "ms": stages[k], "achieved_gbs": b / (stages[k] * 1e-3) / 1e9,
+                "frac": b / (stages[k] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+            for k, b in sbytes.items()}
 
     # The pair sort alone (astro_radix_sort) on uniform keys of the step's
-    # width and length, after an L2 flush: the sort stage's HBM roofline.
-    from astro_gb300.radix_sort import RadixSort
-
-    g = torch.Generator(device="cuda").manual_seed(w.seed)
-    keys = torch.randint(0, 1 << 62, (n,), device="cuda", generator=g, dtype=torch.int64)
-    if key_bits < 63:
-        keys &= (1 << key_bits) - 1
-    keys_out = torch.empty_like(keys)
-    idx_out = torch.empty(n, dtype=torch.int32, device="cuda")
-    sorter = RadixSort(n, key_bits)
-    sort_ms = []
-    for it in range(4):
-        with torch.cuda.stream(stream):
-            flush.fill_(3)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            sorter.sort(keys, None, keys_out, idx_out, n, stream=sim.stream)
-            e1.record(stream)
-        sim.synchronize()
-        if it:
-            sort_ms.append(e0.elapsed_time(e1))
-    passes = (key_bits + 7) // 8
-    sort_b = (8 + 24 * passes - 4) * n
-    sort_roofline = {"bound": "hbm", "key_bits": key_bits, "passes": passes, "keys": n,
-                     "bytes": sort_b, "ms": float(np.mean(sort_ms)),
-                     "achieved": sort_b / (np.mean(sort_ms) * 1e-3) / 1e9,
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": sort_b / (np.mean(sort_ms) * 1e-3) / 1e9 / peaks["hbm_gbs"]}
-    del keys, keys_out, idx_out, sorter
+    # width and length, after an L2 flush: the sort stage's HBM roofline
+    # (PHYSICAL workloads; the reference's scene sorts only its 205 tree bodies).
+    sort_roofline = None
+    if not is_ref:
+        sort_roofline = sort_alone(torch, n, key_bits, w.seed, flush, stream, sim, peaks)
     quad = (p.flags & L.FLAG_QUADRUPOLE) != 0
+
     flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * cell_inter + \
         FLOPS_PER_INTERACTION * (interactions - cell_inter)
 
@@ -388,17 +413,21 @@ def run_ours(args, world, rank, local):
     fp32_peak = 2 * 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     achieved = flops / (trav * 1e-3) / 1e12
 
-    # Error against the FP64 direct sum on sampled particles (current state).
-    rng = np.random.default_rng(w.seed)
-    samples = np.sort(rng.choice(n, size=min(args.error_samples, n), replace=False)).astype(np.uint32)
-    sim.generate_morton_codes()
-    sim.sort()
-    sim.build_tree()
-    sim.barnes_hut()
-    acc = sim.read_accel()
-    direct = sim.direct_accel_f64(samples)
-    sim.update_spheres(0.0)
-    err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    # Error against the FP64 direct sum on sampled particles (current state;
+    # PHYSICAL units only).
+    err = None
+    if not is_ref:
+        rng = np.random.default_rng(w.seed)
+        samples = np.sort(rng.choice(n, size=min(args.error_samples, n), replace=False)).astype(
+            np.uint32)
+        sim.generate_morton_codes()
+        sim.sort()
+        sim.build_tree()
+        sim.barnes_hut()
+        acc = sim.read_accel()
+        direct = sim.direct_accel_f64(samples)
+        sim.update_spheres(0.0)
+        err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
 
     # End to end through the C ABI with pinned host buffers.
     e2e = None
@@ -409,8 +438,8 @@ def run_ours(args, world, rank, local):
         hvr = pin_vr.numpy().view(L.VELOCITY_RADIUS)
         hpm[:] = pm
         hvr[:] = vr
-        up = ((lambda: sim.upload_systems(hpm, hvr, sizes)) if sizes
-              else (lambda: sim.upload(hpm, hvr)))
+        def up():
+            upload_from(hpm, hvr)
         for _ in range(max(1, args.warmup)):
             up()
             sim.draw(dt, 1)
@@ -483,6 +512,16 @@ def run_ours(args, world, rank, local):
 
 # ----------------------------------------------------------- CPU side --
 
+def cpu_step(orc, w, p, pm_c, vr_c, sizes, dt):
+    """One step of the CPU restatement in place (64 one-bit split passes per
+    sort, as the reference)."""
+    if w.preset == "reference":
+        ct, n_tree = w.make_colors()
+        orc.ref_run(p, pm_c, vr_c, ct, n_tree=n_tree, dt=dt, steps=1, split_passes=64)
+    else:
+        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+
+
 def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
     """The CPU restatement on all host cores: whole steps of the same
     workload until the time budget is spent (at least one)."""
@@ -491,9 +530,10 @@ def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
     cores = orc.set_threads(args.cpu_threads)
     steps, t_total = 0, 0.0
     pm_c, vr_c = pm.copy(), vr.copy()
+    w = WORKLOADS[args.workload]
     while True:
         t0 = time.perf_counter()
-        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+        cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
         t_total += time.perf_counter() - t0
         steps += 1
         if t_total >= budget_s:
@@ -519,10 +559,10 @@ def run_reference(args):
     cores = orc.set_threads(args.cpu_threads)
     pm_c, vr_c = pm.copy(), vr.copy()
     for _ in range(args.warmup):
-        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+        cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        orc.phys_run(p, pm_c, vr_c, sizes=sizes, dt=dt, steps=1, split_passes=64)
+        cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
     t = time.perf_counter() - t0
     value = n * args.steps / t
     sample = f"{args.steps} whole steps of the workload (N={n}), 64 one-bit split passes per sort"
@@ -539,8 +579,10 @@ def run_reference(args):
 
 
 def config_dict(args, desc, n, dt, p, knob_source):
-    walk = "per-particle" if p.flags & 0x20 else "group"
-    return {"workload": f"{args.workload}: {desc}", "n": n, "preset": "PHYSICAL",
+    walk = ("per-particle (the reference's)" if p.preset == 0
+            else "per-particle" if p.flags & 0x20 else "group")
+    return {"workload": f"{args.workload}: {desc}", "n": n,
+            "preset": "PHYSICAL" if p.preset == 1 else "REFERENCE",
             "form": args.form, "walk": walk, "quadrupole": bool(p.flags & 0x10),
             "opening": "size/theta + delta" if p.flags & 0x8 else "size/theta",
             "theta": p.theta, "eps": p.softening, "dt": dt, "G": p.g,
@@ -590,9 +632,9 @@ def main():
                          "launch_ms": r["trav_ms"],
                          "peak_source": f"2 x 128 FP32 lanes x SMs x sm_max_mhz ({r['peak_src']} peaks file)"},
             "cpu_baseline": cpu, "clocks": r["clocks"],
-            "error_vs_fp64_direct": {"median": float(np.median(r["err"])),
-                                     "p99": float(np.percentile(r["err"], 99)),
-                                     "samples": int(len(r["err"]))},
+            "error_vs_fp64_direct": None if r["err"] is None else {
+                "median": float(np.median(r["err"])), "p99": float(np.percentile(r["err"], 99)),
+                "samples": int(len(r["err"]))},
             "interactions_per_particle": r["interactions"] / r["n"],
             "cell_interactions_per_particle": r["cell_inter"] / r["n"],
             "node_visits_per_particle": r["visits"] / r["n"],

@@ -13,10 +13,11 @@ ROOT = Path(__file__).resolve().parents[1]
 def test_workloads_match_their_descriptions():
     from astro_gb300.workloads import WORKLOADS
 
-    assert sorted(WORKLOADS) == ["c1", "c2", "c3", "c4", "c5"]
+    assert sorted(WORKLOADS) == ["c1", "c2", "c3", "c4", "c5", "ref"]
+    assert WORKLOADS["ref"].preset == "reference" and WORKLOADS["ref"].lbits == 6
     assert WORKLOADS["c2"].n == 524288 and WORKLOADS["c5"].n == 1 << 24
     assert WORKLOADS["c4"].generator == "batch"
-    assert len({w.seed for w in WORKLOADS.values()}) == 5
+    assert len({w.seed for w in WORKLOADS.values()}) == 6
 
 
 def test_autotune_candidates_stay_in_range():
