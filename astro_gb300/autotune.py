@@ -10,7 +10,7 @@ The knobs are fields of astro_params that change speed, not physics:
   bucket        leaf tile size: an opened node holding <= bucket particles
                 is summed particle by particle
   sort_variant  radix sort pass kernel (items per thread / blocks per SM /
-                ranking)
+                ranking / pipelined)
 
 theta, the softening, the quadrupole and opening-radius flags and the form
 (plain / precision) are physics and stay as given.
@@ -59,7 +59,7 @@ def candidates(knob: str, n: int) -> list[int]:
     if knob == "block_warps":
         return [4, 8]
     if knob == "sort_variant":
-        return list(range(1, 8))
+        return list(range(1, 10))
     raise KeyError(knob)
 
 

@@ -348,9 +348,11 @@ __device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint
     return __fmul_rn(crit, crit);
 }
 
-// PHYSICAL centre of mass (and mass) from the raw sums: one correctly rounded
-// reciprocal of the mass and three products (FP64 in the precision form,
-// then rounded to FP32); zero for a massless node.
+// PHYSICAL centre of mass (and mass) from the raw sums: one reciprocal of
+// the mass and three products; zero for a massless node. FP32: a correctly
+// rounded reciprocal. Precision form: the FP32 reciprocal refined by one
+// FP64 Newton step, r = r0 + r0 (1 - m r0) (about 46 bits, two FMAs instead
+// of an FP64 division), then FP64 products rounded to FP32.
 __device__ __forceinline__ float4 com_from_sums(float sx, float sy, float sz, float m) {
     if (!(m > 0.f)) return make_float4(0.f, 0.f, 0.f, m);
     const float inv = __fdiv_rn(1.0f, m);
@@ -358,7 +360,8 @@ __device__ __forceinline__ float4 com_from_sums(float sx, float sy, float sz, fl
 }
 __device__ __forceinline__ float4 com_from_sums(double sx, double sy, double sz, double m) {
     if (!(m > 0.0)) return make_float4(0.f, 0.f, 0.f, __double2float_rn(m));
-    const double inv = __ddiv_rn(1.0, m);
+    const double r0 = (double)__fdiv_rn(1.0f, __double2float_rn(m));
+    const double inv = __fma_rn(r0, __fma_rn(-m, r0, 1.0), r0);
     return make_float4(__double2float_rn(__dmul_rn(sx, inv)), __double2float_rn(__dmul_rn(sy, inv)),
                        __double2float_rn(__dmul_rn(sz, inv)), __double2float_rn(m));
 }
@@ -373,7 +376,8 @@ __device__ __forceinline__ void emit_group(const AggArgs& a, uint32_t b, uint32_
 //   sums of m and x*m in sorted order; the last leaf sums [start, numUnique)
 //   as the reference does (Octree.metal:71).
 // kMode 1 (PHYSICAL plain): state already in sorted order; raw FP32 sums.
-// kMode 2 (PHYSICAL precision): FP64 sums of m and m*(x64 - origin).
+// kMode 2 (PHYSICAL precision): FP64 sums of m and m*x over the FP32
+//   positions relative to the system origin.
 template <int kMode>
 __global__ void aggregate_leaf_kernel(AggArgs a) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -408,18 +412,29 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
         reinterpret_cast<float4*>(a.node_sum)[j] = make_float4(sx, sy, sz, m);
         cm = com_from_sums(sx, sy, sz, m);
     } else {
-        const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
-        const double ox = a.sys[s].origin[0], oy = a.sys[s].origin[1], oz = a.sys[s].origin[2];
+        // FP64 sums of m * x over the FP32 positions relative to the system
+        // origin (written by the encode from the FP64 master copy): the
+        // product of two floats is exact in FP64, so each FMA rounds once,
+        // exactly as a multiply-then-add would.
         double m = 0, sx = 0, sy = 0, sz = 0;
         for (uint32_t i = pb; i < pe; ++i) {
-            const double mi = (double)a.pos[i].w;
+            const float4 q = a.pos[i];
+            const double mi = (double)q.w;
             m = __dadd_rn(m, mi);
-            sx = __dadd_rn(sx, __dmul_rn(mi, __dsub_rn(a.x64[i], ox)));
-            sy = __dadd_rn(sy, __dmul_rn(mi, __dsub_rn(a.x64[(size_t)a.n + i], oy)));
-            sz = __dadd_rn(sz, __dmul_rn(mi, __dsub_rn(a.x64[2 * (size_t)a.n + i], oz)));
+            sx = __fma_rn(mi, (double)q.x, sx);
+            sy = __fma_rn(mi, (double)q.y, sy);
+            sz = __fma_rn(mi, (double)q.z, sz);
         }
         reinterpret_cast<double4*>(a.node_sum)[j] = make_double4(sx, sy, sz, m);
-        cm = com_from_sums(sx, sy, sz, m);
+        if (pe - pb == 1 && m >= 1.17549435e-38) {
+            // One particle of normal FP32 mass: the sums are m*x exactly and
+            // the reciprocal is within 2^-47 of 1/m, so the FP32 centre of
+            // mass is x itself (+0 for -0, as the sums give).
+            const float4 q = a.pos[pb];
+            cm = make_float4(__fadd_rn(q.x, 0.f), __fadd_rn(q.y, 0.f), __fadd_rn(q.z, 0.f), q.w);
+        } else {
+            cm = com_from_sums(sx, sy, sz, m);
+        }
     }
     a.node_cm[j] = cm;
     a.node_rng[j] = make_uint4(0u, 0u, pb, pe);
@@ -485,6 +500,16 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
         }
         if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
         else cm.w = m;
+    } else if (nch == 1) {
+        // One child (most nodes of the lower layers): every sum is the
+        // child's (0 + s is exact, and no sum is -0 since all start at +0),
+        // so the sums, the centre of mass and the moments equal the child's;
+        // copying them is what the arithmetic below would produce.
+        if (kMode == 1)
+            reinterpret_cast<float4*>(a.node_sum)[node] = reinterpret_cast<const float4*>(a.node_sum)[cb];
+        else
+            reinterpret_cast<double4*>(a.node_sum)[node] = reinterpret_cast<const double4*>(a.node_sum)[cb];
+        cm = need_ccm ? ccm[0] : a.node_cm[cb];
     } else if (kMode == 1) {
         const float4* sum = reinterpret_cast<const float4*>(a.node_sum);
         float4 cs[8];
@@ -523,7 +548,10 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
     a.node_cm[node] = cm;
     a.node_rng[node] = make_uint4(cb, ce, pb, pe);
     if (kMode != 0) {
-        if (a.want_quad) {
+        if (a.want_quad && nch == 1) {
+            a.node_q[node] = a.node_q[cb];
+            a.node_qyz[node] = a.node_qyz[cb];
+        } else if (a.want_quad) {
             float4 qc[8];
             float qyz[8];
 #pragma unroll

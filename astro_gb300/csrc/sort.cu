@@ -15,6 +15,7 @@
 //      as contiguous stores.
 // A stable LSD sort yields the one stable permutation, so the result equals
 // the reference's bit by bit, including the order of equal keys.
+#include <algorithm>
 #include <cstdlib>
 
 #include "common.cuh"
@@ -256,22 +257,236 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     }
 }
 
-// Pass-kernel variants (items per thread, blocks per SM, ranking).
+// ------------------------------------------------------ pipelined pass ----
+// Persistent blocks. Each block takes the ticket of its next tile before it
+// ranks the current one and has that tile's keys (and values) brought into
+// shared memory by bulk asynchronous copies (cp.async.bulk completing on an
+// mbarrier), so the load of tile t+1 overlaps the ranking, look-back and
+// scatter of tile t. Only whole tiles whose source addresses are 16-byte
+// aligned are copied this way; the last, partial tile is read directly.
+// Tickets keep their order, so a tile's look-back only waits on tiles that
+// running blocks hold and finish first. Every wait is bounded.
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for the phase of the given parity; false (and the error bit)
+// after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
+    for (uint32_t polls = 0; polls < kSpinLimit; ++polls) {
+        if (mbar_test(bar, parity)) return true;
+        if (polls > 64) __nanosleep(32);
+    }
+    atomicOr(err, kErrLookbackTimeout);
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <int kItems>
+struct PipeSmem {
+    static constexpr int kTile = kThreads * kItems;
+    uint64_t keys[2][kTile];  // tile buffers; the current one is reused as the scatter stage
+    uint32_t vals[2][kTile];
+    uint32_t warp_hist[kWarps][kRadix];
+    uint32_t tile_start[kRadix];
+    uint32_t global_base[kRadix];
+    uint32_t scan_tmp[kWarps];
+    uint32_t tile_next;
+    uint32_t pad;
+    uint64_t bar[2];
+};
+
+template <int kItems, int kMinBlocks>
+__global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kernel(
+    const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+    uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+    const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
+    uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
+    uint32_t digit_bits, uint32_t* __restrict__ err) {
+    using Smem = PipeSmem<kItems>;
+    constexpr int kTile = Smem::kTile;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = d_count ? min(*d_count, n_est) : n_est;
+    const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    const uint32_t nfull = n / kTile;  // tiles fetched by bulk copies
+    const uint32_t dmask = (1u << digit_bits) - 1u;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t tx_bytes = kTile * 8u + (vals_in ? kTile * 4u : 0u);
+
+    if (tid == 0) {
+        mbar_init(&sm.bar[0]);
+        mbar_init(&sm.bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sm.tile_next = atomicAdd(tile_counter, 1u);
+    }
+    __syncthreads();
+    uint32_t cur = sm.tile_next;
+    if (cur >= ntiles) return;
+    // Thread 0 issues the copies; phase and pending bits are kept by every
+    // thread (all of them wait).
+    auto issue = [&](uint32_t t, uint32_t buf) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sm.bar[buf], tx_bytes);
+        bulk_load(sm.keys[buf], keys_in + (size_t)t * kTile, kTile * 8u, &sm.bar[buf]);
+        if (vals_in) bulk_load(sm.vals[buf], vals_in + (size_t)t * kTile, kTile * 4u, &sm.bar[buf]);
+    };
+    // Per-buffer bits: the mbarrier phase parity to wait for, and whether a
+    // copy into the buffer is in flight.
+    uint32_t phase = 0u, pending = 0u;
+    uint32_t b = 0;
+    if (cur < nfull) {
+        if (tid == 0) issue(cur, 0);
+        pending |= 1u;
+    }
+    while (true) {
+        if (tid == 0) sm.tile_next = atomicAdd(tile_counter, 1u);
+        for (uint32_t i = tid; i < kWarps * kRadix; i += kThreads) (&sm.warp_hist[0][0])[i] = 0;
+        __syncthreads();
+        const uint32_t next = sm.tile_next;
+        if (next < nfull) {
+            if (tid == 0) issue(next, b ^ 1u);
+            pending |= 1u << (b ^ 1u);
+        }
+        const uint64_t tile_base = (uint64_t)cur * kTile;
+        const uint32_t warp_off = warp * 32u * kItems;
+        uint64_t key[kItems];
+        uint32_t val[kItems], pos[kItems];
+        if ((pending >> b) & 1u) {
+            mbar_wait(&sm.bar[b], (phase >> b) & 1u, err);
+            phase ^= 1u << b;
+            pending &= ~(1u << b);
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                const uint32_t li = warp_off + 32u * k + lane;
+                key[k] = sm.keys[b][li];
+                val[k] = vals_in ? sm.vals[b][li] : (uint32_t)(tile_base + li);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                const uint64_t i = tile_base + warp_off + 32ull * k + lane;
+                const bool valid = i < n;
+                key[k] = valid ? __ldcs(keys_in + i) : ~0ull;
+                val[k] = valid ? (vals_in ? __ldcs(vals_in + i) : (uint32_t)i) : 0u;
+            }
+        }
+        // Ranking with per-bit ballots, in item order (stable).
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = tile_base + warp_off + 32ull * k + lane;
+            const bool valid = i < n;
+            const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
+            const uint32_t peers = peer_mask(digit, digit_bits, __ballot_sync(kFullMask, valid));
+            const uint32_t lower = __popc(peers & lt), cnt = __popc(peers);
+            uint32_t old = 0;
+            if (valid) old = sm.warp_hist[warp][digit];
+            __syncwarp();
+            if (valid && lower + 1 == cnt) sm.warp_hist[warp][digit] = old + cnt;
+            __syncwarp();
+            pos[k] = old + lower;
+        }
+        __syncthreads();
+        uint32_t tile_cnt = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = sm.warp_hist[w][tid];
+            sm.warp_hist[w][tid] = tile_cnt;
+            tile_cnt += c;
+        }
+        uint32_t* my_word = lookback + (size_t)cur * kRadix + tid;
+        st_relaxed_u32(my_word, (cur == 0 ? kLbInclusive : kLbAggregate) | tile_cnt);
+        const uint32_t tile_start = block_exclusive_scan(tile_cnt, sm.scan_tmp);
+        sm.tile_start[tid] = tile_start;
+        uint32_t prefix = 0;
+        if (cur > 0) {
+            prefix = lookback_window(lookback, cur, tid, err);
+            st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
+        }
+        sm.global_base[tid] = excl[tid] + prefix;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
+            pos[k] += sm.tile_start[digit] + sm.warp_hist[warp][digit];
+        }
+        // The current buffer is free (its contents are in registers): stage
+        // the tile there in sorted order.
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = tile_base + warp_off + 32ull * k + lane;
+            if (i < n) {
+                sm.keys[b][pos[k]] = key[k];
+                sm.vals[b][pos[k]] = val[k];
+            }
+        }
+        __syncthreads();
+        const uint32_t tile_n = (uint32_t)min((uint64_t)kTile, (uint64_t)n - tile_base);
+        for (uint32_t i = tid; i < tile_n; i += kThreads) {
+            const uint64_t kk = sm.keys[b][i];
+            const uint32_t digit = (uint32_t)(kk >> shift) & dmask;
+            const uint32_t o = sm.global_base[digit] + (i - sm.tile_start[digit]);
+            keys_out[o] = kk;
+            vals_out[o] = sm.vals[b][i];
+        }
+        __syncthreads();
+        if (next >= ntiles) break;
+        cur = next;
+        b ^= 1u;
+    }
+    // A copy is only left in flight if a wait gave up; wait for it (bounded)
+    // before the block's shared memory is released.
+    for (uint32_t k = 0; k < 2; ++k)
+        if ((pending >> k) & 1u) mbar_wait(&sm.bar[k], (phase >> k) & 1u, err);
+}
+
+// Pass-kernel variants (items per thread, blocks per SM, ranking; the
+// pipelined ones run persistent blocks and need 16-byte aligned inputs).
 struct PassVariant {
     int items;
     void (*kernel)(const uint64_t*, const uint32_t*, uint64_t*, uint32_t*, const uint32_t*, uint32_t,
                    const uint32_t*, uint32_t*, uint32_t*, uint32_t, uint32_t, uint32_t*);
     size_t smem;
+    bool pipelined;
 };
 const PassVariant kVariants[] = {
-    {16, sort_pass_kernel<16, 2, false>, sizeof(PassSmem<16>)},
-    {16, sort_pass_kernel<16, 2, true>, sizeof(PassSmem<16>)},
-    {12, sort_pass_kernel<12, 3, true>, sizeof(PassSmem<12>)},
-    {8, sort_pass_kernel<8, 4, true>, sizeof(PassSmem<8>)},
-    {20, sort_pass_kernel<20, 2, true>, sizeof(PassSmem<20>)},
-    {12, sort_pass_kernel<12, 3, false>, sizeof(PassSmem<12>)},
-    {8, sort_pass_kernel<8, 4, false>, sizeof(PassSmem<8>)},
+    {16, sort_pass_kernel<16, 2, false>, sizeof(PassSmem<16>), false},
+    {16, sort_pass_kernel<16, 2, true>, sizeof(PassSmem<16>), false},
+    {12, sort_pass_kernel<12, 3, true>, sizeof(PassSmem<12>), false},
+    {8, sort_pass_kernel<8, 4, true>, sizeof(PassSmem<8>), false},
+    {20, sort_pass_kernel<20, 2, true>, sizeof(PassSmem<20>), false},
+    {12, sort_pass_kernel<12, 3, false>, sizeof(PassSmem<12>), false},
+    {8, sort_pass_kernel<8, 4, false>, sizeof(PassSmem<8>), false},
+    {12, sort_pass_pipelined_kernel<12, 2>, sizeof(PipeSmem<12>), true},
+    {8, sort_pass_pipelined_kernel<8, 3>, sizeof(PipeSmem<8>), true},
 };
+constexpr int kFallbackVariant = 5;  // for inputs a pipelined variant cannot copy
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 constexpr int kMinItems = 8;  // sizes the look-back words for every variant
 static_assert(kThreads * kMinItems == (int)kSortPlanTile, "look-back sizing");
@@ -349,9 +564,22 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
         return cudaErrorInvalidValue;
     cudaError_t e0 = sort_init();
     if (e0 != cudaSuccess) return e0;
-    const PassVariant& pv = kVariants[variant == 0 ? g_variant : (int)variant - 1];
+    int vi = variant == 0 ? g_variant : (int)variant - 1;
+    // Bulk copies need 16-byte aligned sources; the temporaries always are.
+    if (kVariants[vi].pipelined &&
+        (((uintptr_t)keys_in | (uintptr_t)(vals_in ? vals_in : nullptr)) & 15u) != 0)
+        vi = kFallbackVariant;
+    const PassVariant& pv = kVariants[vi];
     const uint32_t tile = (uint32_t)(kThreads * pv.items);
     const uint32_t ntiles = (uint32_t)(((uint64_t)n_est + tile - 1) / tile);
+    uint32_t grid = ntiles;
+    if (pv.pipelined) {
+        int per_sm = 0;
+        cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pv.kernel, kThreads,
+                                                                       pv.smem);
+        if (eo != cudaSuccess) return eo;
+        grid = std::min<uint32_t>(ntiles, (uint32_t)std::max(1, per_sm) * (uint32_t)num_sms());
+    }
     char* base = static_cast<char*>(temp);
     uint64_t* keys_tmp = reinterpret_cast<uint64_t*>(base + plan.keys_tmp);
     uint32_t* vals_tmp = reinterpret_cast<uint32_t*>(base + plan.vals_tmp);
@@ -375,7 +603,7 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
         uint32_t* vout = to_out ? vals_out : vals_tmp;
         const uint32_t shift = 8u * p;
         const uint32_t bits = key_bits == 0 ? 0u : std::min(8u, key_bits - shift);
-        pv.kernel<<<ntiles, kThreads, pv.smem, st>>>(
+        pv.kernel<<<grid, kThreads, pv.smem, st>>>(
             kin, vin, kout, vout, d_count, n_est, excl + p * kRadix,
             lookback + (size_t)p * plan.ntiles * kRadix, counters + p, shift, bits, err);
         kin = kout;

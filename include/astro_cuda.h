@@ -177,7 +177,10 @@ typedef struct astro_params {
                                  per SM / ranking): 0 = library default,
                                  1 = 16/2/ballot, 2 = 16/2/match, 3 = 12/3/match,
                                  4 = 8/4/match, 5 = 20/2/match, 6 = 12/3/ballot,
-                                 7 = 8/4/ballot */
+                                 7 = 8/4/ballot; 8 = 12/2 and 9 = 8/3 ballot with
+                                 persistent blocks that bulk-copy the next tile
+                                 while ranking the current one (16-byte aligned
+                                 inputs; others use 6) */
     uint32_t light_sources;   /* REFERENCE: astro_step runs the lighting pass
                                  with the first light_sources particles (at most
                                  5) as lights (Renderer.swift:539; numStars = 5);

@@ -263,13 +263,14 @@ struct PhysState {
                 if (prec) {
                     double sx = 0, sy = 0, sz = 0, m = 0;
                     if (l == 0) {
+                        // FP64 sums over the FP32 frame relative to the system
+                        // origin; float x float products are exact in FP64.
                         for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
-                            uint32_t s = sys_of[i];
-                            double mi = (double)pos[4ull * i + 3];
+                            double mi = (double)rel[4ull * i + 3];
                             m += mi;
-                            sx += mi * (x64[3ull * i + 0] - quant[s].origin[0]);
-                            sy += mi * (x64[3ull * i + 1] - quant[s].origin[1]);
-                            sz += mi * (x64[3ull * i + 2] - quant[s].origin[2]);
+                            sx += mi * (double)rel[4ull * i + 0];
+                            sy += mi * (double)rel[4ull * i + 1];
+                            sz += mi * (double)rel[4ull * i + 2];
                         }
                     } else {
                         for (uint32_t c = cbeg[node]; c < cend[node]; ++c) {
@@ -284,9 +285,14 @@ struct PhysState {
                     o[1] = sy;
                     o[2] = sz;
                     o[3] = m;
-                    // Centre of mass through one reciprocal of the mass.
+                    // Centre of mass through one reciprocal of the mass: the
+                    // FP32 reciprocal refined by one FP64 Newton step.
                     float* c = &cm[4ull * node];
-                    const double inv = m > 0 ? 1.0 / m : 0.0;
+                    double inv = 0.0;
+                    if (m > 0) {
+                        const double r0 = (double)(1.0f / (float)m);
+                        inv = std::fma(r0, std::fma(-m, r0, 1.0), r0);
+                    }
                     c[0] = m > 0 ? (float)(sx * inv) : 0.0f;
                     c[1] = m > 0 ? (float)(sy * inv) : 0.0f;
                     c[2] = m > 0 ? (float)(sz * inv) : 0.0f;

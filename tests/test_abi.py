@@ -128,7 +128,7 @@ def test_argument_errors_without_device(native):
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(group_size=33)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
-    bad = p.replace(sort_variant=8)
+    bad = p.replace(sort_variant=10)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(light_sources=5)  # lighting needs the REFERENCE preset
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1

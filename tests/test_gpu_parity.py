@@ -193,7 +193,7 @@ def test_physical_fast_within_tolerance(ag, oracle, walk, warps, persistent):
 
 @pytest.mark.parametrize("group_size,sort_variant,form", [(8, 1, 0), (16, 4, 1), (1, 7, 0),
                                                          (32, 6, 1), (5, 2, 0), (24, 3, 0),
-                                                         (12, 5, 0)])
+                                                         (12, 5, 0), (32, 8, 0), (20, 9, 1)])
 def test_group_size_and_sort_variant_bit_exact(ag, oracle, group_size, sort_variant, form):
     """Particles per warp and the sort's pass kernel are tuning knobs: every
     setting must give the oracle's tree and accelerations bit for bit."""
@@ -485,3 +485,103 @@ def test_splat_bit_exact(ag, oracle, width, height, pos):
     assert np.array_equal(rgba, want_rgba)
     assert np.array_equal(rgba2, rgba) and np.array_equal(depth2, depth)
     assert (depth < 1.0).sum() > 100
+
+
+_PIPELINED_SORT_CHECK = r"""
+import sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from astro_gb300.radix_sort import RadixSort
+rng = np.random.default_rng(5)
+for n, bits in [(1, 64), (3071, 18), (3072, 18), (6144 * 3 + 5, 64), (1 << 20, 26), (5_000_001, 63)]:
+    keys = rng.integers(0, 1 << min(bits, 63), n, dtype=np.uint64)
+    keys[rng.integers(0, n, n // 3)] = keys[0]
+    for off in (0, 1):  # 1: an input starting 8 bytes into a buffer (the fallback kernel)
+        buf = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+        buf[off:off + n] = torch.from_numpy(keys.view(np.int64)).cuda()
+        dk = buf[off:off + n]
+        idx = torch.from_numpy(rng.permutation(n).astype(np.int32)).cuda()
+        ok = torch.empty(n, dtype=torch.int64, device="cuda")
+        oi = torch.empty(n, dtype=torch.int32, device="cuda")
+        RadixSort(n, bits).sort(dk, idx, ok, oi, n)
+        torch.cuda.synchronize()
+        order = np.argsort(keys, kind="stable")
+        assert np.array_equal(ok.cpu().numpy().view(np.uint64), keys[order]), (n, bits, off)
+        assert np.array_equal(oi.cpu().numpy(), idx.cpu().numpy()[order]), (n, bits, off)
+print("ok")
+"""
+
+
+@pytest.mark.parametrize("variant_index", [7, 8])
+def test_pipelined_sort_variants_match_stable_argsort(ag, tmp_path, variant_index):
+    """The pipelined pass kernels (sort_variant 8 and 9, selected here as the
+    library default through ASTRO_SORT_VARIANT in a fresh process): whole and
+    partial tiles, given indices, and unaligned inputs that fall back."""
+    import os
+    import subprocess
+    import sys
+
+    script = tmp_path / "check.py"
+    script.write_text(_PIPELINED_SORT_CHECK)
+    env = dict(os.environ, ASTRO_SORT_VARIANT=str(variant_index))
+    root = str(Path(__file__).resolve().parents[1])
+    res = subprocess.run([sys.executable, str(script), root], capture_output=True, text=True,
+                         env=env, timeout=600)
+    assert res.returncode == 0 and "ok" in res.stdout, res.stderr[-2000:]
+
+
+# ------------------------------------------------------ degenerate inputs --
+
+def _degenerate(case):
+    rng = np.random.default_rng(3)
+    if case == "one":
+        return np.array([[0.5, -0.25, 2.0]])
+    if case == "two":
+        return np.array([[0.0, 0.0, 0.0], [1e-3, 0.0, 0.0]])
+    if case == "coincident":   # a zero-extent box: every key equal, one leaf
+        return np.full((1000, 3), 0.25)
+    if case == "line":         # two zero extents
+        return np.stack([np.linspace(-1, 1, 3000), np.zeros(3000), np.zeros(3000)], axis=1)
+    if case == "sheet":        # one zero extent, random in the plane
+        xy = rng.uniform(-1, 1, (5000, 2))
+        return np.concatenate([xy, np.zeros((5000, 1))], axis=1)
+    raise KeyError(case)
+
+
+@pytest.mark.parametrize("case", ["one", "two", "coincident", "line", "sheet"])
+@pytest.mark.parametrize("form", [0, 1])
+def test_degenerate_inputs_bit_exact(ag, oracle, case, form):
+    """Boxes of zero extent in some or all axes, a single particle, and many
+    coincident particles (one leaf): same tree, forces and state as the CPU
+    restatement, and finite everywhere."""
+    L = ag.layouts
+    pos = _degenerate(case)
+    pm, vr = particles(L, pos, masses=np.full(len(pos), 1.0 / len(pos)))
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=10, form=form, softening=0.01,
+                          flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.isfinite(out["acc4"]).all() and np.isfinite(out["pm"]["position"]).all()
+    assert np.array_equal(out["pm"], pm_o)
+    n = len(pos)
+    assert out["interactions"] == ref["interactions"] and out["interactions"] <= n * (n - 1) + n
+
+
+def test_reference_coincident_bodies_bit_exact(ag, oracle):
+    """REFERENCE preset: tree bodies sharing one position (one key, one
+    leaf) and dust on top of them."""
+    L = ag.layouts
+    pos = np.concatenate([np.full((8, 3), 1e5), np.full((50, 3), 1e5)])
+    pm, vr = particles(L, pos, masses=np.full(len(pos), 1000.0))
+    ct = np.zeros(len(pos), L.COLOR_TYPE)
+    ct["type"] = [1] * 8 + [2] * 50
+    p = ag.default_params(L.PRESET_REFERENCE)
+    out = run_gpu(ag, p, pm, vr, ct=ct, n_tree=8, dt=1.0 / 60, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.ref_run(p, pm_o, vr_o, ct, n_tree=8, dt=1.0 / 60, steps=2, split_passes=64)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o)

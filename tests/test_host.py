@@ -28,7 +28,7 @@ def test_autotune_candidates_stay_in_range():
         assert c == sorted(c) and all(3 <= v <= 21 for v in c)
     assert autotune.candidates("group_size", 1000)[-1] == 32
     assert set(autotune.candidates("block_warps", 1)) <= {2, 4, 8}
-    assert autotune.candidates("sort_variant", 1) == list(range(1, 8))
+    assert autotune.candidates("sort_variant", 1) == list(range(1, 10))
     with pytest.raises(KeyError):
         autotune.candidates("theta", 1)
 
