@@ -25,8 +25,8 @@ struct TopoArgs {
 struct AggArgs {
     const uint64_t* sorted_keys;
     const uint32_t* perm;      // REFERENCE: sorted slot -> upload index
-    const float4* pos;         // REFERENCE: upload order; PHYSICAL: sorted order
-    const double* x64;         // precision form, sorted order
+    const float4* pos;         // REFERENCE: upload order; PHYSICAL: sorted order (the
+                               // precision form's FP32 frame relative to the origin)
     const SysInfo* sys;
     const uint32_t* pbeg;
     const uint32_t* node_cbeg;

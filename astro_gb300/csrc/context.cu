@@ -264,7 +264,6 @@ int stage_build(astro_ctx* ctx) {
     a.sorted_keys = ctx->sorted_keys;
     a.perm = ctx->perm;
     a.pos = is_phys(ctx) ? ctx->pos[1] : ctx->pos[0];
-    a.x64 = ctx->x64[1];
     a.sys = ctx->sys;
     a.pbeg = ctx->node_pbeg;
     a.node_cbeg = ctx->node_cbeg;

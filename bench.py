@@ -296,7 +296,6 @@ def run_ours(args, world, rank, local):
     import torch
 
     import astro_gb300 as ag
-    from astro_gb300 import ic
     from astro_gb300 import layouts as L
 
     torch.cuda.set_device(local)
@@ -546,7 +545,6 @@ def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
 def run_reference(args):
     """--impl reference: the CPU restatement timed on the host cores."""
     import astro_gb300 as ag
-    from astro_gb300 import ic
     from astro_gb300 import layouts as L
     from oracle import oracle as orc
 
