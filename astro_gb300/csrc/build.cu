@@ -330,7 +330,7 @@ __device__ __forceinline__ void quad_add(float q[5], float m, float dx, float dy
     q[4] = __fadd_rn(q[4], __fmul_rn(m, __fmul_rn(ty, dz)));
 }
 
-// Opening radius^2 of a node: (size / theta + |com - cell centre|)^2, the
+// Opening radius^2 of a node: (size / theta + w |com - cell centre|)^2, the
 // cell found from the node's key prefix in its system's box.
 __device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint32_t l, float4 cm) {
     const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
@@ -344,7 +344,7 @@ __device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint
     const float cz = __fadd_rn(si.lo[2], __fmul_rn((float)(2u * compact3_21(code >> 2) + 1u), half));
     const float dx = __fsub_rn(cm.x, cx), dy = __fsub_rn(cm.y, cy), dz = __fsub_rn(cm.z, cz);
     const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    const float crit = __fadd_rn(__fdiv_rn(size, a.theta), __fsqrt_rn(dd));
+    const float crit = __fadd_rn(__fdiv_rn(size, a.theta), __fmul_rn(a.delta_weight, __fsqrt_rn(dd)));
     return __fmul_rn(crit, crit);
 }
 

@@ -46,6 +46,7 @@ struct AggArgs {
     uint32_t want_quad;
     uint32_t want_delta;
     float theta;
+    float delta_weight;    // w of the opening radius size/theta + w delta
     uint32_t group_size;   // particles per group walk, 1..kGroupSize
     uint32_t* err;         // device error word (kErrBadLayer: a node with > 8 children)
 };

@@ -88,6 +88,8 @@ int validate_params(const astro_params* p, const char** why) {
     if (p->group_size > 32) return (*why = "group_size must be in [0, 32]", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->sort_variant > astro::sort_variant_count())
         return (*why = "unknown sort_variant", ASTRO_ERR_INVALID_ARGUMENT);
+    if (!(p->open_delta_weight >= 0.0f) || !std::isfinite(p->open_delta_weight))
+        return (*why = "open_delta_weight must be finite and >= 0", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->light_sources > 0 && p->preset != ASTRO_PRESET_REFERENCE)
         return (*why = "the lighting pass needs the REFERENCE preset", ASTRO_ERR_INVALID_ARGUMENT);
     return ASTRO_OK;
@@ -282,6 +284,7 @@ int stage_build(astro_ctx* ctx) {
     a.want_quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.want_delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
     a.theta = ctx->p.theta;
+    a.delta_weight = ctx->p.open_delta_weight;
     a.group_size = ctx->p.group_size ? ctx->p.group_size : astro::kGroupSize;
     a.err = ctx->err;
     CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
@@ -453,6 +456,7 @@ int astro_params_default(uint32_t preset, astro_params* out) {
     out->form = ASTRO_FORM_PLAIN;
     out->lbits = 6;                 // MortonCode.metal:47-50
     out->theta = 0.7f;              // Renderer.swift:864
+    out->open_delta_weight = 1.0f;
     out->force_clamp = 1e5f;        // BarnesHut.metal:100
     if (preset == ASTRO_PRESET_REFERENCE) {
         out->g = 1e11f;             // BarnesHut.metal:39

@@ -75,7 +75,8 @@ class Params(ctypes.Structure):
         ("group_size", ctypes.c_uint32),
         ("sort_variant", ctypes.c_uint32),
         ("light_sources", ctypes.c_uint32),
-        ("_reserved", ctypes.c_uint32 * 3),
+        ("open_delta_weight", ctypes.c_float),
+        ("_reserved", ctypes.c_uint32 * 2),
     ]
 
     def replace(self, **kw) -> "Params":

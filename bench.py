@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--warps", type=int, default=None)
     ap.add_argument("--group-size", type=int, default=None)
     ap.add_argument("--sort-variant", type=int, default=None)
+    ap.add_argument("--delta-weight", type=float, default=None,
+                    help="w of the opening radius size/theta + w |com - cell centre|")
     ap.add_argument("--no-tuned", action="store_true", help="ignore the autotuner's file")
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--persistent", action="store_true")
@@ -102,9 +104,10 @@ def knobs(args):
 
         tuned = autotune.load().get(f"{args.workload}/{args.form}", {}).get("knobs", {})
     default = {"lbits": WORKLOADS[args.workload].lbits, "bucket": 16, "block_warps": 0,
-               "group_size": 0, "sort_variant": 0}
+               "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0}
     given = {"lbits": args.lbits, "bucket": args.bucket, "block_warps": args.warps,
-             "group_size": args.group_size, "sort_variant": args.sort_variant}
+             "group_size": args.group_size, "sort_variant": args.sort_variant,
+             "open_delta_weight": args.delta_weight}
     out, source = {}, {}
     for k in default:
         if given[k] is not None:
@@ -582,10 +585,12 @@ def config_dict(args, desc, n, dt, p, knob_source):
     return {"workload": f"{args.workload}: {desc}", "n": n,
             "preset": "PHYSICAL" if p.preset == 1 else "REFERENCE",
             "form": args.form, "walk": walk, "quadrupole": bool(p.flags & 0x10),
-            "opening": "size/theta + delta" if p.flags & 0x8 else "size/theta",
+            "opening": (f"size/theta + {p.open_delta_weight:g} delta" if p.flags & 0x8
+                        else "size/theta"),
             "theta": p.theta, "eps": p.softening, "dt": dt, "G": p.g,
             "lbits": p.lbits, "bucket": p.bucket, "group_size": p.group_size or 32,
             "block_warps": p.block_warps or 4, "sort_variant": p.sort_variant,
+            "open_delta_weight": p.open_delta_weight,
             "knob_source": knob_source,
             "l2": "flushed (256 MB write) before every timed step",
             "parallelism": "replicas (one independent system per GPU)"}

@@ -185,7 +185,11 @@ typedef struct astro_params {
                                  with the first light_sources particles (at most
                                  5) as lights (Renderer.swift:539; numStars = 5);
                                  0 = no lighting pass */
-    uint32_t _reserved[3];
+    float open_delta_weight;  /* PHYSICAL with ASTRO_FLAG_OPEN_DELTA: a node opens
+                                 unless the distance exceeds
+                                 size/theta + w |com - cell centre| (default 1;
+                                 0 = size/theta) */
+    uint32_t _reserved[2];
 } astro_params;
 
 /* Fill *out with the defaults of a preset. */

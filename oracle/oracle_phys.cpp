@@ -617,7 +617,8 @@ struct PhysState {
 
     // Quadrupole moments about each node's centre of mass (parallel-axis
     // sums over children, traceless: Qzz = -Qxx - Qyy) and the
-    // delta-corrected opening radius (size / theta + |com - cell centre|)^2.
+    // delta-corrected opening radius (size / theta + w |com - cell centre|)^2,
+    // w = params.open_delta_weight.
     void moments() {
         const bool want_q = (p.flags & kFlagQuad) != 0, want_d = (p.flags & kFlagDelta) != 0;
         if (!want_q && !want_d) return;
@@ -665,7 +666,7 @@ struct PhysState {
                         d[a] = c[a] - center;
                     }
                     float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-                    float crit = size / p.theta + std::sqrt(dd);
+                    float crit = size / p.theta + p.open_delta_weight * std::sqrt(dd);
                     ncrit2[node] = crit * crit;
                 }
             }

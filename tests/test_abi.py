@@ -57,6 +57,7 @@ _Static_assert(offsetof(OctreeNode, layer) == 112, "layer");
 _Static_assert(offsetof(astro_params, block_warps) == 60, "block_warps");
 _Static_assert(offsetof(astro_params, group_size) == 64, "group_size");
 _Static_assert(offsetof(astro_params, sort_variant) == 68, "sort_variant");
+_Static_assert(offsetof(astro_params, open_delta_weight) == 76, "open_delta_weight");
 _Static_assert(sizeof(astro_params) == 88, "astro_params");
 _Static_assert(sizeof(astro_state_header) == 136, "astro_state_header");
 _Static_assert(offsetof(astro_state_header, params) == 16, "state params");
@@ -111,7 +112,7 @@ def test_params_defaults(native):
     assert list(p.type_accel_scale) == [5.0, 5.0, 1.0]
     assert p.light_sources == 5  # numStars (Renderer.swift:26)
     assert lib().astro_params_default(L.PRESET_PHYSICAL, byref(p)) == 0
-    assert p.g == 1.0 and p.bucket == 16 and p.light_sources == 0
+    assert p.g == 1.0 and p.bucket == 16 and p.light_sources == 0 and p.open_delta_weight == 1.0
     assert lib().astro_params_default(7, byref(p)) == -1
 
 
@@ -129,6 +130,8 @@ def test_argument_errors_without_device(native):
     bad = p.replace(group_size=33)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(sort_variant=10)
+    assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
+    bad = p.replace(open_delta_weight=-1.0)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(light_sources=5)  # lighting needs the REFERENCE preset
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1

@@ -585,3 +585,21 @@ def test_reference_coincident_bodies_bit_exact(ag, oracle):
     assert_tree_equal(out, ref)
     assert np.array_equal(out["acc4"], ref["acc4"])
     assert np.array_equal(out["pm"], pm_o)
+
+
+@pytest.mark.parametrize("weight,form", [(0.0, 0), (0.5, 1), (0.7, 0)])
+def test_delta_weight_bit_exact(ag, oracle, weight, form):
+    """The weight of the opening radius' delta term changes the walk; every
+    weight must reproduce the CPU restatement bit for bit."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=12, form=form, open_delta_weight=weight,
+                          softening=0.005, flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    pm, vr = ic.disk_bulge(16384, seed=1002)
+    out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=5e-4, steps=2)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]

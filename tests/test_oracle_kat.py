@@ -19,7 +19,7 @@ def ref_params(**kw):
     """REFERENCE defaults without loading the CUDA library."""
     p = L.Params(preset=L.PRESET_REFERENCE, form=0, lbits=6, flags=0, theta=0.7, g=1e11,
                  softening=0.01, leaf_min_dist2=50.0, force_clamp=1e5, quant_offset=1e6,
-                 damping=0.9995, bucket=0, block_warps=0)
+                 damping=0.9995, bucket=0, block_warps=0, open_delta_weight=1.0)
     p.type_accel_scale[0], p.type_accel_scale[1], p.type_accel_scale[2] = 5.0, 5.0, 1.0
     return p.replace(**kw) if kw else p
 
@@ -28,7 +28,7 @@ def phys_params(**kw):
     p = L.Params(preset=L.PRESET_PHYSICAL, form=0, lbits=6,
                  flags=L.FLAG_OPEN_DELTA | L.FLAG_QUADRUPOLE, theta=0.7, g=1.0,
                  softening=0.01, leaf_min_dist2=0.0, force_clamp=1e5, quant_offset=0.0,
-                 damping=1.0, bucket=16, block_warps=0)
+                 damping=1.0, bucket=16, block_warps=0, open_delta_weight=1.0)
     for i in range(3):
         p.type_accel_scale[i] = 1.0
     return p.replace(**kw) if kw else p
@@ -342,3 +342,16 @@ def test_splat_points_discs_depth_and_blending(oracle):
     vr["radius"] = 2.0
     rgba, depth = oracle.splat(pm, vr, ct[:1], cam, W, H)
     assert (depth == 1.0).all()
+
+
+def test_delta_weight_zero_is_the_plain_opening_radius(oracle, native):
+    # w = 0 turns size/theta + w delta into size/theta exactly: the same walk
+    # and forces as without the delta flag; a larger w opens more nodes.
+    from astro_gb300 import ic
+
+    pm, vr = ic.disk_bulge(6000, seed=2)
+    no_delta = oracle.phys_run(phys_params(flags=L.FLAG_QUADRUPOLE), pm.copy(), vr.copy(), dt=0.0)
+    w0 = oracle.phys_run(phys_params(open_delta_weight=0.0), pm.copy(), vr.copy(), dt=0.0)
+    w1 = oracle.phys_run(phys_params(), pm.copy(), vr.copy(), dt=0.0)
+    assert np.array_equal(no_delta["acc4"], w0["acc4"])
+    assert no_delta["interactions"] == w0["interactions"] < w1["interactions"]
