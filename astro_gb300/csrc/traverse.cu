@@ -516,27 +516,26 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                         const float dx = c.x - me.x, dy = c.y - me.y, dz = c.z - me.z;
                         const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
                         const float u = inv * inv, inv3 = u * inv;
-                        float ex, ey, ez;
                         if constexpr (kQuad) {
-                            // inv^3 [(M + 5/2 u^2 d.Qd) d - u Qd], u = 1/r^2.
+                            // inv^3 (M + 5/2 u^2 d.Qd) d - inv^5 Qd, u = 1/r^2:
+                            // two FMAs per component into the sums.
                             const float4 q = cs.q;
                             const float4 q2 = cs.q2;
                             const float qx = fmaf(q.x, dx, fmaf(q.z, dy, q.w * dz));
                             const float qy = fmaf(q.z, dx, fmaf(q.y, dy, q2.x * dz));
                             const float qz = fmaf(q.w, dx, fmaf(q2.x, dy, q2.y * dz));
                             const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
-                            const float s1 = fmaf(2.5f * u * u, dqd, c.w);
-                            ex = fmaf(s1, dx, -u * qx);
-                            ey = fmaf(s1, dy, -u * qy);
-                            ez = fmaf(s1, dz, -u * qz);
+                            const float sa = inv3 * fmaf(2.5f * u * u, dqd, c.w);
+                            const float sb = -(inv3 * u);
+                            rx = fmaf(sb, qx, fmaf(sa, dx, rx));
+                            ry = fmaf(sb, qy, fmaf(sa, dy, ry));
+                            rz = fmaf(sb, qz, fmaf(sa, dz, rz));
                         } else {
-                            ex = c.w * dx;
-                            ey = c.w * dy;
-                            ez = c.w * dz;
+                            const float sa = inv3 * c.w;
+                            rx = fmaf(sa, dx, rx);
+                            ry = fmaf(sa, dy, ry);
+                            rz = fmaf(sa, dz, rz);
                         }
-                        rx = fmaf(inv3, ex, rx);
-                        ry = fmaf(inv3, ey, ry);
-                        rz = fmaf(inv3, ez, rz);
                     };
                     if (reps == 1) {
 #pragma unroll 4
