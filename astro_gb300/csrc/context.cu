@@ -636,15 +636,25 @@ int astro_set_params(astro_ctx* ctx, const astro_params* params) {
     return ASTRO_OK;
 }
 
+static int upload_particles(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                            const ColorType* ct, uint32_t n, uint32_t n_tree);
+
 static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
                          const ColorType* ct, uint32_t n, uint32_t n_tree,
                          const std::vector<uint32_t>& sizes) {
     cudaStream_t st = ctx->stream;
     const bool phys = is_phys(ctx), prec = is_prec(ctx);
-    drop_graph(ctx);
-    ctx->uploaded = false;
+    // New particles in the same layout (counts, system sizes, depth) as the
+    // last upload: the buffers, the system records' layout fields and the
+    // captured step stay valid (every data-dependent field is recomputed by
+    // each step), so only the particles are copied in.
+    const bool same_layout = ctx->uploaded && n == ctx->n && n_tree == ctx->n_tree &&
+                             sizes == ctx->sys_sizes && ctx->lbits == ctx->p.lbits;
     ctx->tree_valid = false;
     ctx->state_in_b = false;
+    if (same_layout) return upload_particles(ctx, pm, vr, ct, n, n_tree);
+    drop_graph(ctx);
+    ctx->uploaded = false;
     ctx->n = n;
     ctx->n_tree = n_tree;
     ctx->nsys = (uint32_t)sizes.size();
@@ -693,7 +703,15 @@ static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityR
         CK(cudaMemcpyAsync(ctx->bbox64, lo64.data(), lo64.size() * 8, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));  // the host vectors go out of scope
     }
-    // Particles through the staging buffer.
+    return upload_particles(ctx, pm, vr, ct, n, n_tree);
+}
+
+// The particle copy of an upload: host arrays through the staging buffer into
+// the state (A) buffers, ids 0..n-1, types and colours.
+static int upload_particles(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                            const ColorType* ct, uint32_t n, uint32_t n_tree) {
+    cudaStream_t st = ctx->stream;
+    const bool phys = is_phys(ctx), prec = is_prec(ctx);
     char* stg = static_cast<char*>(ctx->staging);
     PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
     VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);

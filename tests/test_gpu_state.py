@@ -102,3 +102,31 @@ def test_driver_resume_gives_identical_state_files(ag, tmp_path, scene):
     assert b[-1]["step"] == 4
     assert (tmp_path / "a" / "step_000004.state").read_bytes() == \
         (tmp_path / "b" / "step_000004.state").read_bytes()
+
+
+def test_reupload_in_the_same_layout_reuses_the_step(ag):
+    """Uploading new particles in the layout of the last upload keeps the
+    captured step; the result equals a fresh context's, and a different layout
+    still rebuilds everything."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, softening=0.005, lbits=12)
+    a_pm, a_vr = ic.disk_bulge(20000, seed=1)
+    b_pm, b_vr = ic.plummer(20000, seed=2)
+    c_pm, c_vr = ic.plummer(12345, seed=3)
+    with ag.Simulation(p, max_n=20000) as sim:
+        sim.upload(a_pm, a_vr)
+        sim.draw(1e-3, 2)
+        sim.upload(b_pm, b_vr)          # same layout
+        sim.draw(1e-3, 3)
+        got_b = sim.download()
+        sim.upload(c_pm, c_vr)          # smaller: a new layout
+        sim.draw(1e-3, 3)
+        got_c = sim.download()
+    for (pm, vr), got in [((b_pm, b_vr), got_b), ((c_pm, c_vr), got_c)]:
+        with ag.Simulation(p, max_n=20000) as fresh:
+            fresh.upload(pm, vr)
+            fresh.draw(1e-3, 3)
+            want = fresh.download()
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
