@@ -59,6 +59,7 @@ SIGNATURES = {
     "astro_read_accel": (c_int, [c_void_p, c_void_p, c_uint32]),
     "astro_read_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64),
                                  POINTER(c_uint64)]),
+    "astro_read_far_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
     "astro_direct_accel_f64": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "astro_lighting": (c_int, [c_void_p, c_uint32]),
     "astro_splat": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),

@@ -12,10 +12,15 @@ The knobs are fields of astro_params that change speed, not physics:
   sort_variant  radix sort pass kernel (items per thread / blocks per SM /
                 ranking / pipelined)
 
+  far_ratio     accepted nodes further than (group radius) / far_ratio from
+                the group's centre are summed through one second-order
+                expansion per group instead of per particle: larger ratios
+                expand more nodes and cost accuracy
   open_delta_weight
                 w of the opening radius size/theta + w |com - cell centre|:
-                lower w opens fewer nodes and costs accuracy, so it is only
-                lowered while the error stays within 0.8 x the target
+                lower w opens fewer nodes and costs accuracy
+far_ratio and open_delta_weight are only moved while the error stays within
+0.8 x the target.
 
 theta, the softening, the quadrupole and opening-radius flags and the form
 (plain / precision) are physics and stay as given.
@@ -24,7 +29,7 @@ Search: coordinate descent from the preset's defaults. Each knob in turn is
 swept with the others fixed; the fastest setting is kept among those whose
 median relative acceleration error against the FP64 direct sum (on sampled
 particles) is at most max(target, 1.02 x the starting error) (0.8 x the target
-for open_delta_weight). A step's time is
+for the accuracy knobs). A step's time is
 the CUDA-event time of graph-replayed steps (dt = 0, so every trial sees the
 same particles); the sort variant is judged by the sort stage's own time.
 
@@ -49,8 +54,9 @@ from .simulation import Simulation, default_params
 from .workloads import WORKLOADS
 
 TUNED_PATH = Path(__file__).resolve().parent / "tuned.json"
-KNOBS = ("lbits", "bucket", "group_size", "block_warps", "sort_variant", "open_delta_weight")
-ACCURACY_KNOBS = ("open_delta_weight",)
+KNOBS = ("lbits", "bucket", "group_size", "block_warps", "sort_variant", "far_ratio",
+         "open_delta_weight")
+ACCURACY_KNOBS = ("far_ratio", "open_delta_weight")
 FORMS = {"plain": L.FORM_PLAIN, "precision": L.FORM_PRECISION}
 
 
@@ -67,6 +73,8 @@ def candidates(knob: str, n: int) -> list[int]:
         return [4, 8]
     if knob == "sort_variant":
         return list(range(1, 10))
+    if knob == "far_ratio":
+        return [0.1, 0.15, 0.2, 0.25, 0.3]
     if knob == "open_delta_weight":
         return [0.85, 0.7, 0.5]
     raise KeyError(knob)
@@ -143,7 +151,7 @@ def tune(workload: str, form: str, target: float = 1e-3, steps: int | None = Non
          log=print) -> dict:
     t = Trial(workload, FORMS[form])
     start = {"lbits": t.w.lbits, "bucket": 16, "group_size": 32, "block_warps": 4,
-             "sort_variant": 0, "open_delta_weight": 1.0}
+             "sort_variant": 0, "far_ratio": 0.0, "open_delta_weight": 1.0}
     if not steps:
         # About 60 ms of timed steps per trial.
         steps = int(np.clip(60.0 / t.run(start, 3)["ms"], 3, 60))

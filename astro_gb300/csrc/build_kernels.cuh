@@ -110,6 +110,7 @@ struct TraverseArgs {
     uint32_t* frontier;       // per-warp ping-pong buffers, 2 * frontier_cap each
     uint32_t frontier_cap;
     uint32_t nsys;
+    float far2;               // group walk: far_ratio^2 (0: no far nodes)
 };
 
 cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,

@@ -29,6 +29,9 @@ using astro::SysInfo;
 namespace {
 
 constexpr const char* kVersion = "astro_gb300 1.0 (sm_103a)";
+// Traversal counters: interactions, node visits, cell interactions, far
+// nodes, far interactions.
+constexpr int kNumStats = 5;
 
 int fail(astro_ctx* ctx, int code, const char* what) {
     if (ctx) ctx->last_error = what;
@@ -90,6 +93,8 @@ int validate_params(const astro_params* p, const char** why) {
         return (*why = "unknown sort_variant", ASTRO_ERR_INVALID_ARGUMENT);
     if (!(p->open_delta_weight >= 0.0f) || !std::isfinite(p->open_delta_weight))
         return (*why = "open_delta_weight must be finite and >= 0", ASTRO_ERR_INVALID_ARGUMENT);
+    if (!(p->far_ratio >= 0.0f && p->far_ratio <= 0.5f))
+        return (*why = "far_ratio must be in [0, 0.5]", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->light_sources > 0 && p->preset != ASTRO_PRESET_REFERENCE)
         return (*why = "the lighting pass needs the REFERENCE preset", ASTRO_ERR_INVALID_ARGUMENT);
     return ASTRO_OK;
@@ -193,11 +198,13 @@ bool group_walk(const astro_ctx* ctx) {
 }
 
 // Frontier scratch of the group walk: two buffers of frontier_cap node
-// indices per resident warp of the persistent launch.
+// indices per resident warp of the persistent launch, and a third for the
+// far-node list when params.far_ratio > 0.
 int ensure_frontier(astro_ctx* ctx) {
     if (!group_walk(ctx)) return ASTRO_OK;
     astro::TraverseConfig c = traverse_config(ctx);
-    const size_t words = (size_t)astro::group_walk_warps(c) * 2 * ctx->frontier_cap;
+    const size_t per_warp = ctx->p.far_ratio > 0.0f ? 3 : 2;
+    const size_t words = (size_t)astro::group_walk_warps(c) * per_warp * ctx->frontier_cap;
     if (words <= ctx->frontier_words) return ASTRO_OK;
     dev_free(ctx->frontier);
     ctx->frontier_words = 0;
@@ -316,6 +323,7 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     a.stats = ctx->stats;
     a.queue = ctx->counters + 1;
     a.delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
+    a.far2 = ctx->p.far_ratio * ctx->p.far_ratio;
     a.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.node_crit2 = ctx->node_crit2;
     a.node_q = ctx->node_q;
@@ -348,7 +356,7 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
 // evaluates forces (the state is copied back to A unchanged).
 int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
     cudaStream_t st = ctx->stream;
-    CK(cudaMemsetAsync(ctx->stats, 0, 3 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(ctx->stats, 0, kNumStats * sizeof(unsigned long long), st));
     if (!is_phys(ctx)) {
         if (ctx->n_tree == 0) {
             CK(cudaMemsetAsync(ctx->acc, 0, sizeof(float4) * ctx->n, st));
@@ -531,7 +539,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     CKC(dev_alloc(&ctx->counters, 16));
     CKC(dev_alloc(&ctx->groups, max_n));
     CKC(dev_alloc(&ctx->err, 1));
-    CKC(dev_alloc(&ctx->stats, 3));
+    CKC(dev_alloc(&ctx->stats, kNumStats));
     CKC(dev_alloc(&ctx->layer_count, ASTRO_MAX_LAYERS));
     CKC(dev_alloc(&ctx->sys, max_systems));
     CKC(dev_alloc(&ctx->bbox32, 6ull * max_systems));
@@ -540,7 +548,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     CKC(dev_alloc(&ctx->chunks, ctx->chunk_capacity));
     CKC(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
     CKC(cudaMemset(ctx->layer_count, 0, sizeof(uint32_t) * ASTRO_MAX_LAYERS));
-    CKC(cudaMemset(ctx->stats, 0, 3 * sizeof(unsigned long long)));
+    CKC(cudaMemset(ctx->stats, 0, kNumStats * sizeof(unsigned long long)));
     if (params->form == ASTRO_FORM_PRECISION && ensure_x64(ctx) != ASTRO_OK)
         return cleanup(ASTRO_ERR_OUT_OF_MEMORY);
 #undef CKC
@@ -937,6 +945,16 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
     if (interactions) *interactions = s[0];
     if (node_visits) *node_visits = s[1];
     if (cell_interactions) *cell_interactions = s[2];
+    return r;
+}
+
+int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions) {
+    NEED_UPLOAD();
+    unsigned long long s[kNumStats] = {0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(s, ctx->stats, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
+    int r = check_device(ctx);
+    if (far_nodes) *far_nodes = s[3];
+    if (far_interactions) *far_interactions = s[4];
     return r;
 }
 

@@ -142,7 +142,8 @@ struct astro_ctx {
     size_t topo_lookback_words = 0;
     uint32_t* counters = nullptr;             // [0] topology tiles, [1] traversal queue, [2] groups
     uint32_t* err = nullptr;                  // device error word
-    unsigned long long* stats = nullptr;      // interactions, node visits
+    unsigned long long* stats = nullptr;      // interactions, node visits, cell
+                                              // interactions, far nodes, far interactions
     void* readback = nullptr;
     size_t readback_bytes = 0;
 

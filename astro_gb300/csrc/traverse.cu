@@ -161,6 +161,174 @@ __device__ __forceinline__ void particle_term(float dx, float dy, float dz, floa
     }
 }
 
+// ---------------------------------------------------------- far nodes ----
+// The field of an accepted node at d = D - rho, D = com - group centre, to
+// second order in the offset rho (the same terms as cell_term, without G):
+//   a_i(D - rho) = a_i - J_ij rho_j + 1/2 H_ijk rho_j rho_k
+// With R = (|D|^2 + eps^2)^(-1/2), q = QD, s = D.QD:
+//   a_i   = al D_i - R^5 q_i
+//   J_ij  = ga (q_i D_j + q_j D_i) - be D_i D_j - R^5 Q_ij + al [i=j]
+//   H_ijk = nu D_i D_j D_k + ka S(qDD) + ga (S(QD) + S(q delta)) - be S(delta D)
+// al = m R^3 + 5/2 s R^7, be = 3 m R^5 + 35/2 s R^9, ga = 5 R^7,
+// ka = -35 R^9, nu = 15 m R^7 + 315/2 s R^11; S(.) sums the three distinct
+// placements of the indices. Coefficients: a {x, y, z}, J {xx, yy, zz, xy,
+// xz, yz}, H {xxx, yyy, zzz, xxy, xxz, xyy, yyz, xzz, yzz, xyz}. kExact
+// rounds every product and sum separately in the CPU restatement's order
+// (fma(a, b, c) there is a * b + c); otherwise FMAs and rsqrt are used.
+constexpr int kFarCoefs = 19;
+
+template <bool kExact>
+__device__ __forceinline__ float xmul(float a, float b) { return kExact ? __fmul_rn(a, b) : a * b; }
+template <bool kExact>
+__device__ __forceinline__ float xadd(float a, float b) { return kExact ? __fadd_rn(a, b) : a + b; }
+template <bool kExact>
+__device__ __forceinline__ float xfma(float a, float b, float c) {
+    return kExact ? __fadd_rn(__fmul_rn(a, b), c) : fmaf(a, b, c);
+}
+
+struct FarTerms {
+    float D[3], qv[3], Q[3][3], R5, al, be, ga, ka, nu;
+};
+
+template <bool kExact, int i, int j>
+__device__ __forceinline__ float far_j(const FarTerms& f) {
+    float v = xfma<kExact>(f.ga, xfma<kExact>(f.qv[i], f.D[j], xmul<kExact>(f.qv[j], f.D[i])),
+                           -xfma<kExact>(f.be, xmul<kExact>(f.D[i], f.D[j]),
+                                         xmul<kExact>(f.R5, f.Q[i][j])));
+    if (i == j) v = xadd<kExact>(v, f.al);
+    return v;
+}
+
+template <bool kExact, int i, int j, int k>
+__device__ __forceinline__ float far_h(const FarTerms& f) {
+    const float dij = xmul<kExact>(f.D[i], f.D[j]);
+    const float sqdd = xfma<kExact>(
+        f.qv[i], xmul<kExact>(f.D[j], f.D[k]),
+        xfma<kExact>(f.qv[j], xmul<kExact>(f.D[i], f.D[k]), xmul<kExact>(f.qv[k], dij)));
+    const float sqd = xfma<kExact>(f.Q[i][j], f.D[k],
+                                   xfma<kExact>(f.Q[i][k], f.D[j], xmul<kExact>(f.Q[j][k], f.D[i])));
+    const float ddd = xmul<kExact>(dij, f.D[k]);
+    if constexpr (kExact) {
+        // The restatement multiplies by the 0/1 Kronecker factors.
+        constexpr float cij = i == j ? 1.f : 0.f, cik = i == k ? 1.f : 0.f, cjk = j == k ? 1.f : 0.f;
+        const float sqdel = xfma<true>(cjk, f.qv[i], xfma<true>(cik, f.qv[j], __fmul_rn(cij, f.qv[k])));
+        const float sdel = xfma<true>(cij, f.D[k], xfma<true>(cik, f.D[j], __fmul_rn(cjk, f.D[i])));
+        return xfma<true>(f.nu, ddd,
+                          xfma<true>(f.ka, sqdd,
+                                     xfma<true>(f.ga, __fadd_rn(sqd, sqdel), -__fmul_rn(f.be, sdel))));
+    } else if constexpr (i != j && j != k) {
+        // Sorted, all different: no Kronecker terms.
+        return fmaf(f.nu, ddd, fmaf(f.ka, sqdd, f.ga * sqd));
+    } else {
+        // Sorted (i <= j <= k): i = j = k, i = j < k or i < j = k.
+        float sqdel, sdel;
+        if constexpr (i == j && j == k) {
+            sqdel = 3.0f * f.qv[i];
+            sdel = 3.0f * f.D[i];
+        } else if constexpr (i == j) {
+            sqdel = f.qv[k];
+            sdel = f.D[k];
+        } else {
+            sqdel = f.qv[i];
+            sdel = f.D[i];
+        }
+        return fmaf(f.nu, ddd, fmaf(f.ka, sqdd, fmaf(f.ga, sqd + sqdel, -(f.be * sdel))));
+    }
+}
+
+// Adds the far-node coefficients of a node (centre of mass and mass cm,
+// quadrupole {Qxx, Qyy, Qxy, Qxz}, Qyz, Qzz) about the group centre gc into fc.
+template <bool kExact, bool kQuad>
+__device__ __forceinline__ void far_coefs(float4 cm, float4 q, float qyz, float qzz, float gcx,
+                                          float gcy, float gcz, float eps2, float (&fc)[kFarCoefs]) {
+    FarTerms f;
+    f.D[0] = xadd<kExact>(cm.x, -gcx);
+    f.D[1] = xadd<kExact>(cm.y, -gcy);
+    f.D[2] = xadd<kExact>(cm.z, -gcz);
+    const float m = cm.w;
+    const float r2 = xadd<kExact>(
+        xfma<kExact>(f.D[0], f.D[0], xfma<kExact>(f.D[1], f.D[1], xmul<kExact>(f.D[2], f.D[2]))),
+        eps2);
+    const float R = kExact ? __fdiv_rn(1.0f, __fsqrt_rn(r2)) : rsqrtf(r2);
+    const float R2 = xmul<kExact>(R, R), R3 = xmul<kExact>(R2, R), R5 = xmul<kExact>(R3, R2),
+                R7 = xmul<kExact>(R5, R2);
+    f.R5 = R5;
+    if (kQuad || kExact) {
+        const float qxx = kQuad ? q.x : 0.f, qyy = kQuad ? q.y : 0.f, qxy = kQuad ? q.z : 0.f,
+                    qxz = kQuad ? q.w : 0.f, qyz_ = kQuad ? qyz : 0.f, qzz_ = kQuad ? qzz : -0.f;
+        f.Q[0][0] = qxx; f.Q[0][1] = qxy; f.Q[0][2] = qxz;
+        f.Q[1][0] = qxy; f.Q[1][1] = qyy; f.Q[1][2] = qyz_;
+        f.Q[2][0] = qxz; f.Q[2][1] = qyz_; f.Q[2][2] = qzz_;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            f.qv[i] = xfma<kExact>(f.Q[i][0], f.D[0],
+                                   xfma<kExact>(f.Q[i][1], f.D[1], xmul<kExact>(f.Q[i][2], f.D[2])));
+        const float sq = xfma<kExact>(f.D[0], f.qv[0],
+                                      xfma<kExact>(f.D[1], f.qv[1], xmul<kExact>(f.D[2], f.qv[2])));
+        const float R9 = xmul<kExact>(R7, R2), R11 = xmul<kExact>(R9, R2);
+        f.al = xfma<kExact>(m, R3, xmul<kExact>(xmul<kExact>(2.5f, sq), R7));
+        f.be = xfma<kExact>(xmul<kExact>(3.0f, m), R5, xmul<kExact>(xmul<kExact>(17.5f, sq), R9));
+        f.ga = xmul<kExact>(5.0f, R7);
+        f.ka = -xmul<kExact>(35.0f, R9);
+        f.nu = xfma<kExact>(xmul<kExact>(15.0f, m), R7, xmul<kExact>(xmul<kExact>(157.5f, sq), R11));
+    } else {
+        // Monopole only (fast form): Q = 0, q = 0, s = 0.
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            f.qv[i] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) f.Q[i][j] = 0.f;
+        }
+        f.al = m * R3;
+        f.be = 3.0f * m * R5;
+        f.ga = 0.f;
+        f.ka = 0.f;
+        f.nu = 15.0f * m * R7;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        fc[i] = xadd<kExact>(fc[i], xfma<kExact>(f.al, f.D[i], -xmul<kExact>(R5, f.qv[i])));
+    fc[3] = xadd<kExact>(fc[3], far_j<kExact, 0, 0>(f));
+    fc[4] = xadd<kExact>(fc[4], far_j<kExact, 1, 1>(f));
+    fc[5] = xadd<kExact>(fc[5], far_j<kExact, 2, 2>(f));
+    fc[6] = xadd<kExact>(fc[6], far_j<kExact, 0, 1>(f));
+    fc[7] = xadd<kExact>(fc[7], far_j<kExact, 0, 2>(f));
+    fc[8] = xadd<kExact>(fc[8], far_j<kExact, 1, 2>(f));
+    fc[9] = xadd<kExact>(fc[9], far_h<kExact, 0, 0, 0>(f));
+    fc[10] = xadd<kExact>(fc[10], far_h<kExact, 1, 1, 1>(f));
+    fc[11] = xadd<kExact>(fc[11], far_h<kExact, 2, 2, 2>(f));
+    fc[12] = xadd<kExact>(fc[12], far_h<kExact, 0, 0, 1>(f));
+    fc[13] = xadd<kExact>(fc[13], far_h<kExact, 0, 0, 2>(f));
+    fc[14] = xadd<kExact>(fc[14], far_h<kExact, 0, 1, 1>(f));
+    fc[15] = xadd<kExact>(fc[15], far_h<kExact, 1, 1, 2>(f));
+    fc[16] = xadd<kExact>(fc[16], far_h<kExact, 0, 2, 2>(f));
+    fc[17] = xadd<kExact>(fc[17], far_h<kExact, 1, 2, 2>(f));
+    fc[18] = xadd<kExact>(fc[18], far_h<kExact, 0, 1, 2>(f));
+}
+
+// The expansion fc at offset rho from the group centre (without G).
+template <bool kExact>
+__device__ __forceinline__ void far_eval(const float (&fc)[kFarCoefs], float rx, float ry, float rz,
+                                         float& ox, float& oy, float& oz) {
+    const float pxx = xmul<kExact>(rx, rx), pyy = xmul<kExact>(ry, ry), pzz = xmul<kExact>(rz, rz);
+    const float pxy = xmul<kExact>(rx, ry), pxz = xmul<kExact>(rx, rz), pyz = xmul<kExact>(ry, rz);
+    const float* J = fc + 3;
+    const float* H = fc + 9;
+    auto comp = [&](float a, float j0, float j1, float j2, float h0, float h1, float h2, float h3,
+                    float h4, float h5) {
+        const float jr = xfma<kExact>(j0, rx, xfma<kExact>(j1, ry, xmul<kExact>(j2, rz)));
+        const float cross = xfma<kExact>(h3, pxy, xfma<kExact>(h4, pxz, xmul<kExact>(h5, pyz)));
+        const float hh = xfma<kExact>(
+            h0, pxx, xfma<kExact>(h1, pyy, xfma<kExact>(h2, pzz, xmul<kExact>(2.0f, cross))));
+        return xfma<kExact>(0.5f, hh, xadd<kExact>(a, -jr));
+    };
+    // Rows: J {x: xx xy xz, y: xy yy yz, z: xz yz zz}; H {x: xxx xyy xzz xxy xxz xyz,
+    // y: xxy yyy yzz xyy xyz yyz, z: xxz yyz zzz xyz xzz yzz}.
+    ox = comp(fc[0], J[0], J[3], J[4], H[0], H[5], H[7], H[3], H[4], H[9]);
+    oy = comp(fc[1], J[3], J[1], J[5], H[3], H[1], H[8], H[5], H[9], H[6]);
+    oz = comp(fc[2], J[4], J[5], J[2], H[4], H[6], H[2], H[9], H[7], H[8]);
+}
+
 // Per-lane acceleration sum: plain or compensated (Kahan) per component.
 template <bool kExact, bool kKahan>
 struct Accum {
@@ -439,11 +607,12 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
     const uint32_t gw = blockIdx.x * kWarps + warp;
-    uint32_t* buf0 = a.frontier + (size_t)gw * 2 * a.frontier_cap;
+    uint32_t* buf0 = a.frontier + (size_t)gw * (a.far2 > 0.f ? 3 : 2) * a.frontier_cap;
     uint32_t* buf1 = buf0 + a.frontier_cap;
+    uint32_t* far_list = buf1 + a.frontier_cap;
     const uint32_t ngroups = *a.group_count;
     const float g = a.g, eps2 = a.eps2;
-    uint32_t inter = 0, visits = 0, cell_inter = 0;
+    uint32_t inter = 0, visits = 0, cell_inter = 0, far_inter = 0, far_nodes = 0;
 
     while (true) {
         uint32_t gi = 0;
@@ -480,6 +649,19 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
         }
         Accum<kExact, kPrec> cells, leaves;
         uint32_t n_cell = 0, n_leaf = 0;
+
+        // Far nodes: centre and half diagonal of the group's box. The walk
+        // lists far nodes in the warp's third frontier-sized buffer; after
+        // the walk lane l expands far nodes l, l + 32, ... into its partial.
+        const bool far_on = a.far2 > 0.f;
+        const float gcx = __fmul_rn(__fadd_rn(lo_x, hi_x), 0.5f);
+        const float gcy = __fmul_rn(__fadd_rn(lo_y, hi_y), 0.5f);
+        const float gcz = __fmul_rn(__fadd_rn(lo_z, hi_z), 0.5f);
+        const float hrx = __fmul_rn(__fsub_rn(hi_x, lo_x), 0.5f);
+        const float hry = __fmul_rn(__fsub_rn(hi_y, lo_y), 0.5f);
+        const float hrz = __fmul_rn(__fsub_rn(hi_z, lo_z), 0.5f);
+        const float rg2 = __fadd_rn(__fmul_rn(hrx, hrx), __fadd_rn(__fmul_rn(hry, hry), __fmul_rn(hrz, hrz)));
+        uint32_t far_total = 0;
 
         // Cell list: every lane sums its particle against each staged cell.
         // The fast path leaves G out of the terms and applies it once at the end.
@@ -674,11 +856,30 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                 const float bz = fmaxf(fmaxf(__fsub_rn(lo_z, c.z), __fsub_rn(c.z, hi_z)), 0.f);
                 const float dist2 =
                     __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
-                const bool acc = has && dist2 > crit;
-                const bool leaf = has && !acc && (layer == 0 || r.w - r.z <= a.bucket);
-                const bool opn = has && !acc && !leaf;
+                const bool accepted = has && dist2 > crit;
+                const bool leaf = has && !accepted && (layer == 0 || r.w - r.z <= a.bucket);
+                const bool opn = has && !accepted && !leaf;
+                bool far = false;
+                if (far_on && accepted) {
+                    const float Dx = __fsub_rn(c.x, gcx), Dy = __fsub_rn(c.y, gcy),
+                                Dz = __fsub_rn(c.z, gcz);
+                    const float D2 = __fadd_rn(__fmul_rn(Dx, Dx),
+                                               __fadd_rn(__fmul_rn(Dy, Dy), __fmul_rn(Dz, Dz)));
+                    far = __fmul_rn(a.far2, D2) > rg2;
+                }
+                const bool acc = accepted && !far;
                 const uint32_t tested = __popc(__ballot_sync(kFullMask, has));
                 if (owner) visits += tested;
+                // Far nodes, in frontier order.
+                const uint32_t bfar = __ballot_sync(kFullMask, far);
+                if (bfar) {
+                    if (far_total + __popc(bfar) <= a.frontier_cap) {
+                        if (far) far_list[far_total + __popc(bfar & lt)] = nd;
+                        far_total += __popc(bfar);
+                    } else if (lane == 0) {
+                        atomicOr(a.err, kErrFrontier);
+                    }
+                }
                 // Accepted cells, in frontier order.
                 const uint32_t bacc = __ballot_sync(kFullMask, acc);
                 if (bacc) {
@@ -730,6 +931,45 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
         // The self-free fast loop counted the particle's own entry once.
         if (!kExact && eps2 > 0.f && owner) --inter;
 
+        // Far nodes: lane l sums the coefficients of far nodes l, l + 32, ...
+        // in walk order; the partials are combined pairwise (lane l + lane
+        // l^o, o = 16 .. 1), leaving the sum in every lane; each particle
+        // adds the expansion at its offset.
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        if (far_total > 0) {
+            __syncwarp();
+            float fc[kFarCoefs];
+#pragma unroll
+            for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
+            for (uint32_t f = lane; f < far_total; f += 32u) {
+                const uint32_t nd = far_list[f];
+                const float4 c = __ldg(&a.node_cm[nd]);
+                if constexpr (kQuad) {
+                    const float4 q = __ldg(&a.node_q[nd]);
+                    far_coefs<kExact, true>(c, q, __ldg(&a.node_qyz[nd]), -(q.x + q.y), gcx, gcy, gcz,
+                                            eps2, fc);
+                } else {
+                    far_coefs<kExact, false>(c, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, gcx, gcy,
+                                             gcz, eps2, fc);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kFarCoefs; ++k) {
+                float v = fc[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v = xadd<kExact>(v, __shfl_xor_sync(kFullMask, v, o));
+                fc[k] = v;
+            }
+            far_eval<kExact>(fc, xadd<kExact>(me.x, -gcx), xadd<kExact>(me.y, -gcy),
+                             xadd<kExact>(me.z, -gcz), fx, fy, fz);
+            if (owner) {
+                inter += far_total;
+                cell_inter += far_total;
+                far_inter += far_total;
+            }
+            if (lane == 0) far_nodes += far_total;
+        }
+
         float sx, sy, sz;
         if (kExact) {
             cells.finish();
@@ -737,6 +977,11 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             sx = __fadd_rn(cells.ax, leaves.ax);
             sy = __fadd_rn(cells.ay, leaves.ay);
             sz = __fadd_rn(cells.az, leaves.az);
+            if (far_total > 0) {
+                sx = __fadd_rn(sx, __fmul_rn(g, fx));
+                sy = __fadd_rn(sy, __fmul_rn(g, fy));
+                sz = __fadd_rn(sz, __fmul_rn(g, fz));
+            }
         } else {
             // Compensated sums: the running sum minus its pending correction.
             sx = (cells.ax - cells.cx) + (leaves.ax - leaves.cx);
@@ -755,9 +1000,9 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                     }
                 __syncwarp();
             }
-            sx *= g;
-            sy *= g;
-            sz *= g;
+            sx = (sx + fx) * g;
+            sy = (sy + fy) * g;
+            sz = (sz + fz) * g;
         }
         if (owner) {
             const float cl = a.clampv, dt = a.dt;
@@ -785,17 +1030,20 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             }
         }
     }
-    unsigned long long i64 = inter, v64 = visits, c64 = cell_inter;
+    unsigned long long i64 = inter, v64 = visits, c64 = cell_inter, f64 = far_inter;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         i64 += __shfl_xor_sync(kFullMask, i64, o);
         v64 += __shfl_xor_sync(kFullMask, v64, o);
         c64 += __shfl_xor_sync(kFullMask, c64, o);
+        f64 += __shfl_xor_sync(kFullMask, f64, o);
     }
     if (lane == 0) {
         atomicAdd(&a.stats[0], i64);
         atomicAdd(&a.stats[1], v64);
         atomicAdd(&a.stats[2], c64);
+        if (far_nodes) atomicAdd(&a.stats[3], (unsigned long long)far_nodes);
+        if (f64) atomicAdd(&a.stats[4], f64);
     }
 }
 

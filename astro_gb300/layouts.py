@@ -76,7 +76,8 @@ class Params(ctypes.Structure):
         ("sort_variant", ctypes.c_uint32),
         ("light_sources", ctypes.c_uint32),
         ("open_delta_weight", ctypes.c_float),
-        ("_reserved", ctypes.c_uint32 * 2),
+        ("far_ratio", ctypes.c_float),
+        ("_reserved", ctypes.c_uint32 * 1),
     ]
 
     def replace(self, **kw) -> "Params":

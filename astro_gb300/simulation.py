@@ -205,6 +205,12 @@ class Simulation:
         self._check(lib().astro_read_stats(self._h, byref(i), byref(v), byref(c)))
         return (i.value, v.value, c.value) if cells else (i.value, v.value)
 
+    def read_far_stats(self):
+        """(far nodes expanded, far interactions) of the last group walk."""
+        f, fi = c_uint64(), c_uint64()
+        self._check(lib().astro_read_far_stats(self._h, byref(f), byref(fi)))
+        return f.value, fi.value
+
     def direct_accel_f64(self, samples) -> np.ndarray:
         s = np.ascontiguousarray(samples, dtype=np.uint32)
         out = np.zeros((len(s), 3), np.float64)

@@ -44,6 +44,12 @@ UNIT = "particle-updates/s"
 # two vector updates (6), counting an FMA as 2).
 FLOPS_PER_INTERACTION = 20
 FLOPS_PER_QUAD_CELL = 50
+# A far node's expansion about its group's centre: 350 flops once per group
+# (the field, its 6 first and 10 second derivatives from the monopole and
+# quadrupole, and their 19 sums), and 70 per particle of a group with far
+# nodes to evaluate the expansion (3 x (J rho, H rho rho, sums)).
+FLOPS_PER_FAR_NODE = 350
+FLOPS_PER_FAR_EVAL = 70
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one traversal
 # launch, captured with ncu on GB300 for (workload, form, walk) at the tuned
@@ -68,6 +74,9 @@ def parse():
     ap.add_argument("--sort-variant", type=int, default=None)
     ap.add_argument("--delta-weight", type=float, default=None,
                     help="w of the opening radius size/theta + w |com - cell centre|")
+    ap.add_argument("--far-ratio", type=float, default=None,
+                    help="group walk: nodes further than (group radius) / r from the group's "
+                         "centre are summed through one expansion per group (0: none)")
     ap.add_argument("--no-tuned", action="store_true", help="ignore the autotuner's file")
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--persistent", action="store_true")
@@ -104,10 +113,10 @@ def knobs(args):
 
         tuned = autotune.load().get(f"{args.workload}/{args.form}", {}).get("knobs", {})
     default = {"lbits": WORKLOADS[args.workload].lbits, "bucket": 16, "block_warps": 0,
-               "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0}
+               "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0, "far_ratio": 0.0}
     given = {"lbits": args.lbits, "bucket": args.bucket, "block_warps": args.warps,
              "group_size": args.group_size, "sort_variant": args.sort_variant,
-             "open_delta_weight": args.delta_weight}
+             "open_delta_weight": args.delta_weight, "far_ratio": args.far_ratio}
     out, source = {}, {}
     for k in default:
         if given[k] is not None:
@@ -392,8 +401,10 @@ def run_ours(args, world, rank, local):
         sort_roofline = sort_alone(torch, n, key_bits, w.seed, flush, stream, sim, peaks)
     quad = (p.flags & L.FLAG_QUADRUPOLE) != 0
 
-    flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * cell_inter + \
-        FLOPS_PER_INTERACTION * (interactions - cell_inter)
+    far_nodes, far_inter = sim.read_far_stats() if not is_ref else (0, 0)
+    flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * (cell_inter - far_inter) + \
+        FLOPS_PER_INTERACTION * (interactions - cell_inter) + FLOPS_PER_FAR_NODE * far_nodes + \
+        (FLOPS_PER_FAR_EVAL * n if far_nodes else 0)
 
     # Traversal alone, several launches after a flush each, for the roofline.
     trav_ms = []
@@ -504,7 +515,7 @@ def run_ours(args, world, rank, local):
     return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
                 wall=wall,
                 step_ms=step_ms, stages=stages, interactions=interactions, visits=visits,
-                cell_inter=cell_inter, flops=flops,
+                cell_inter=cell_inter, flops=flops, far_nodes=far_nodes, far_inter=far_inter,
                 counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
                 fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
                 launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr,
@@ -590,7 +601,7 @@ def config_dict(args, desc, n, dt, p, knob_source):
             "theta": p.theta, "eps": p.softening, "dt": dt, "G": p.g,
             "lbits": p.lbits, "bucket": p.bucket, "group_size": p.group_size or 32,
             "block_warps": p.block_warps or 4, "sort_variant": p.sort_variant,
-            "open_delta_weight": p.open_delta_weight,
+            "open_delta_weight": p.open_delta_weight, "far_ratio": p.far_ratio,
             "knob_source": knob_source,
             "l2": "flushed (256 MB write) before every timed step",
             "parallelism": "replicas (one independent system per GPU)"}
@@ -623,7 +634,9 @@ def main():
             "data": "synthetic (seeded, Philox4x32-10)",
             "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"], r["knob_source"]),
             "e2e": r["e2e"], "gpu_launches": r["launches"],
-            "roofline": {"kernel": ("traverse_group_kernel" if args.walk == "group"
+            "roofline": {"kernel": ("traverse_ref_kernel"
+                                    if WORKLOADS[args.workload].preset == "reference"
+                                    else "traverse_group_kernel" if args.walk == "group"
                                     else "traverse_phys_kernel"),
                          "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
@@ -640,6 +653,8 @@ def main():
                 "samples": int(len(r["err"]))},
             "interactions_per_particle": r["interactions"] / r["n"],
             "cell_interactions_per_particle": r["cell_inter"] / r["n"],
+            "far_interactions_per_particle": r["far_inter"] / r["n"],
+            "far_nodes": r["far_nodes"],
             "node_visits_per_particle": r["visits"] / r["n"],
             "stages_ms": r["stages"], "stage_roofline_hbm": r["stage_roofline"],
             "sort_roofline": r["sort_roofline"], "layer_counts": r["counts"],

@@ -189,7 +189,15 @@ typedef struct astro_params {
                                  unless the distance exceeds
                                  size/theta + w |com - cell centre| (default 1;
                                  0 = size/theta) */
-    uint32_t _reserved[2];
+    float far_ratio;          /* PHYSICAL group walk: an accepted node whose centre
+                                 of mass lies further than r_g / far_ratio from
+                                 the centre of the group's box (r_g: the box's
+                                 half diagonal) is summed through one
+                                 second-order expansion of its field about that
+                                 centre, evaluated at each particle of the
+                                 group, instead of term by term; 0 = every
+                                 accepted node term by term; 0..0.5 */
+    uint32_t _reserved[1];
 } astro_params;
 
 /* Fill *out with the defaults of a preset. */
@@ -259,6 +267,12 @@ int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n);
  * (accepted node) interactions among them. */
 int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits,
                      uint64_t* cell_interactions);
+
+/* Far-node statistics of the last group walk (params.far_ratio > 0): the
+ * expansions formed (one per group and far node) and, summed over
+ * particles, the accepted nodes evaluated through them (a part of
+ * cell_interactions above). */
+int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions);
 
 /* FP64 direct-sum accelerations (G, eps as the context's PHYSICAL params) of
  * the sampled particles against all particles of their own system, computed

@@ -44,6 +44,8 @@ typedef struct oracle_outputs {
     float* acc4;              /* [n*4] force buffer (float3, 16-byte stride) */
     uint64_t interactions;    /* filled by PHYSICAL runs */
     uint64_t node_visits;
+    uint64_t far_nodes;        /* group walk: expansions formed (group x far node) */
+    uint64_t far_interactions; /* accepted nodes evaluated through them, per particle */
 } oracle_outputs;
 
 /* Number of OpenMP threads used by the oracle (<=0: all). Returns the count in effect. */
@@ -88,6 +90,13 @@ void oracle_lighting(const PositionMass* pm, ColorType* ct, uint32_t n, uint32_t
 void oracle_splat(const PositionMass* pm, const VelocityRadius* vr, const ColorType* ct, uint32_t n,
                   const float* view, const float* proj, const float* cam, uint32_t width,
                   uint32_t height, const float* clear, float* rgba, float* depth);
+
+/* The group walk's far-node expansion: coefficients (a, J, H; 19 floats) of
+ * a node of centre of mass and mass cm4 and quadrupole q5 {Qxx, Qyy, Qxy,
+ * Qxz, Qyz} about gc3, and the expansion times G at offset rho3 (either
+ * output may be NULL). G and eps from p. */
+void oracle_far_expand(const astro_params* p, const float* cm4, const float* q5, const float* gc3,
+                       const float* rho3, float* coefs19, float* acc3);
 
 /* FP64 softened direct sum for sampled particles against their own system. */
 void oracle_direct_accel_f64(const PositionMass* pm, const double* pos64, uint32_t n,

@@ -36,7 +36,7 @@ class Outputs(ctypes.Structure):
         ("codes", c_void_p), ("sorted_codes", c_void_p), ("sorted_indices", c_void_p),
         ("layer_counts", c_void_p), ("layer_sizes", c_void_p), ("layer_offsets", c_void_p),
         ("nodes", c_void_p), ("acc4", c_void_p), ("interactions", c_uint64),
-        ("node_visits", c_uint64),
+        ("node_visits", c_uint64), ("far_nodes", c_uint64), ("far_interactions", c_uint64),
     ]
 
 
@@ -78,6 +78,9 @@ def lib() -> ctypes.CDLL:
         l.oracle_direct_accel_f64.restype = None
         l.oracle_direct_accel_f64.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32,
                                               c_void_p, c_uint32, c_double, c_double, c_void_p]
+        l.oracle_far_expand.restype = None
+        l.oracle_far_expand.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]
         l.oracle_splat.restype = None
         l.oracle_splat.argtypes = [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p,
                                    c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]
@@ -177,9 +180,22 @@ def phys_run(params, pm, vr, sizes=None, dt=1e-3, steps=1, split_passes=0, want_
         raise RuntimeError(f"oracle_phys_run failed ({r})")
     bufs["interactions"] = out.interactions
     bufs["node_visits"] = out.node_visits
+    bufs["far_nodes"] = out.far_nodes
+    bufs["far_interactions"] = out.far_interactions
     if want_pos64:
         bufs["pos64"] = pos64
     return bufs
+
+
+def far_expand(params, cm4, q5, gc3, rho3):
+    """(coefficients[19], G * expansion at rho3) of one far node about gc3."""
+    f = lambda v: np.ascontiguousarray(v, np.float32)
+    cm4, q5, gc3, rho3 = f(cm4), f(q5), f(gc3), f(rho3)
+    co = np.zeros(19, np.float32)
+    acc = np.zeros(3, np.float32)
+    lib().oracle_far_expand(ctypes.addressof(params), _p(cm4), _p(q5), _p(gc3), _p(rho3), _p(co),
+                            _p(acc))
+    return co, acc
 
 
 def direct_accel(pm, samples, g=1.0, eps=0.01, sizes=None, pos64=None) -> np.ndarray:

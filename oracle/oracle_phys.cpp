@@ -82,7 +82,7 @@ struct PhysState {
     std::vector<uint32_t> pbeg, pend, cbeg, cend;
     std::vector<float> quad;     // Qxx, Qyy, Qxy, Qxz, Qyz per node (quadrupole flag)
     std::vector<float> ncrit2;   // per-node opening radius^2 (delta flag)
-    uint64_t interactions = 0, visits = 0;
+    uint64_t interactions = 0, visits = 0, far_nodes = 0, far_interactions = 0;
 
     void layout(const uint32_t* sys_sizes) {
         sys_off.assign(nsys + 1, 0);
@@ -414,6 +414,83 @@ struct PhysState {
         }
     }
 
+    // Far nodes of the group walk. The field of a node (mass m, traceless
+    // quadrupole Q, as in term()) at displacement d = D - rho from a point
+    // rho off the expansion centre, D = com - centre, is taken to second
+    // order in rho:
+    //   a_i(D - rho) = a_i - J_ij rho_j + 1/2 H_ijk rho_j rho_k,
+    // a the field at D, J and H its first and second derivatives. With
+    // R = (|D|^2 + eps^2)^(-1/2), q = QD and s = D.Qd:
+    //   a_i  = al D_i - R^5 q_i
+    //   J_ij = ga (q_i D_j + q_j D_i) - be D_i D_j - R^5 Q_ij + al [i=j]
+    //   H_ijk = nu D_i D_j D_k + ka S(qDD) + ga (S(QD) + S(q delta)) - be S(delta D)
+    // al = m R^3 + 5/2 s R^7, be = 3 m R^5 + 35/2 s R^9, ga = 5 R^7,
+    // ka = -35 R^9, nu = 15 m R^7 + 315/2 s R^11, and S(.) the sum over the
+    // three distinct placements of the indices (S(delta D) = delta_ij D_k +
+    // delta_ik D_j + delta_jk D_i). The 19 coefficients are stored as
+    // a {x, y, z}, J {xx, yy, zz, xy, xz, yz}, H {xxx, yyy, zzz, xxy, xxz,
+    // xyy, yyz, xzz, yzz, xyz}. fma(a, b, c) below is a * b + c with both
+    // operations rounded, the order the CUDA kernels follow.
+    static constexpr int kFarCoefs = 19;
+    static float fma2(float a, float b, float c) { return a * b + c; }
+    void far_coefs(const float* c, const float* q, const float gc[3], float out[kFarCoefs]) const {
+        const float eps2 = p.softening * p.softening;
+        const float D[3] = {c[0] - gc[0], c[1] - gc[1], c[2] - gc[2]};
+        const float m = c[3];
+        const float r2 = fma2(D[0], D[0], fma2(D[1], D[1], D[2] * D[2])) + eps2;
+        const float R = 1.0f / std::sqrt(r2);
+        const float R2 = R * R, R3 = R2 * R, R5 = R3 * R2, R7 = R5 * R2, R9 = R7 * R2,
+                    R11 = R9 * R2;
+        const float Q[3][3] = {{q[0], q[2], q[3]}, {q[2], q[1], q[4]}, {q[3], q[4], -(q[0] + q[1])}};
+        float qv[3];
+        for (int i = 0; i < 3; ++i) qv[i] = fma2(Q[i][0], D[0], fma2(Q[i][1], D[1], Q[i][2] * D[2]));
+        const float sq = fma2(D[0], qv[0], fma2(D[1], qv[1], D[2] * qv[2]));
+        const float al = fma2(m, R3, (2.5f * sq) * R7);
+        const float be = fma2(3.0f * m, R5, (17.5f * sq) * R9);
+        const float ga = 5.0f * R7;
+        const float ka = -(35.0f * R9);
+        const float nu = fma2(15.0f * m, R7, (157.5f * sq) * R11);
+        for (int i = 0; i < 3; ++i) out[i] = fma2(al, D[i], -(R5 * qv[i]));
+        static const int jx[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+        for (int t = 0; t < 6; ++t) {
+            const int i = jx[t][0], j = jx[t][1];
+            float v = fma2(ga, fma2(qv[i], D[j], qv[j] * D[i]), -fma2(be, D[i] * D[j], R5 * Q[i][j]));
+            if (i == j) v = v + al;
+            out[3 + t] = v;
+        }
+        static const int hx[10][3] = {{0, 0, 0}, {1, 1, 1}, {2, 2, 2}, {0, 0, 1}, {0, 0, 2},
+                                      {0, 1, 1}, {1, 1, 2}, {0, 2, 2}, {1, 2, 2}, {0, 1, 2}};
+        for (int t = 0; t < 10; ++t) {
+            const int i = hx[t][0], j = hx[t][1], k = hx[t][2];
+            const float cij = i == j ? 1.0f : 0.0f, cik = i == k ? 1.0f : 0.0f,
+                        cjk = j == k ? 1.0f : 0.0f;
+            const float dij = D[i] * D[j];
+            const float sqdd = fma2(qv[i], D[j] * D[k], fma2(qv[j], D[i] * D[k], qv[k] * dij));
+            const float sqd = fma2(Q[i][j], D[k], fma2(Q[i][k], D[j], Q[j][k] * D[i]));
+            const float sqdel = fma2(cjk, qv[i], fma2(cik, qv[j], cij * qv[k]));
+            const float sdel = fma2(cij, D[k], fma2(cik, D[j], cjk * D[i]));
+            out[9 + t] = fma2(nu, dij * D[k], fma2(ka, sqdd, fma2(ga, sqd + sqdel, -(be * sdel))));
+        }
+    }
+
+    // The expansion of coefficients f about the group centre at offset rho,
+    // times G.
+    void far_eval(const float f[kFarCoefs], const float rho[3], float out[3]) const {
+        const float pxx = rho[0] * rho[0], pyy = rho[1] * rho[1], pzz = rho[2] * rho[2];
+        const float pxy = rho[0] * rho[1], pxz = rho[0] * rho[2], pyz = rho[1] * rho[2];
+        // Per component: J row {j_x, j_y, j_z} and H row {xx, yy, zz, xy, xz, yz}.
+        static const int jr[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+        static const int hr[3][6] = {{0, 5, 7, 3, 4, 9}, {3, 1, 8, 5, 9, 6}, {4, 6, 2, 9, 7, 8}};
+        for (int i = 0; i < 3; ++i) {
+            const float* J = f + 3;
+            const float* H = f + 9;
+            const float jr_ = fma2(J[jr[i][0]], rho[0], fma2(J[jr[i][1]], rho[1], J[jr[i][2]] * rho[2]));
+            const float cross = fma2(H[hr[i][3]], pxy, fma2(H[hr[i][4]], pxz, H[hr[i][5]] * pyz));
+            const float hh = fma2(H[hr[i][0]], pxx, fma2(H[hr[i][1]], pyy, fma2(H[hr[i][2]], pzz, 2.0f * cross)));
+            out[i] = p.g * fma2(0.5f, hh, f[i] - jr_);
+        }
+    }
+
     float node_crit2(uint32_t nd, uint32_t l, uint32_t s) const {
         return (p.flags & kFlagDelta) ? ncrit2[nd] : quant[s].crit2[l];
     }
@@ -530,11 +607,20 @@ struct PhysState {
     // children to the next level. Each particle then sums the accepted cells
     // (in walk order) and, separately, the particles of the listed leaves and
     // buckets (in walk order, itself excluded); a = cells + particles.
+    // With params.far_ratio > 0 an accepted node whose centre of mass lies
+    // further than r_g / far_ratio from the centre of the group's box (r_g
+    // its half diagonal) is a far node: its expansion coefficients
+    // (far_coefs) go into one of 32 partial sums, far node f into partial
+    // f mod 32 in walk order; the partials are combined by the pairwise
+    // exchange 16, 8, 4, 2, 1 (partial l + partial l^o), and each particle
+    // adds the expansion at its offset: a = (cells + particles) + far.
     void traverse_groups() {
         const bool kahan = prec, quad_on = (p.flags & kFlagQuad) != 0;
         const auto groups = make_groups();
-        uint64_t tot_inter = 0, tot_visits = 0;
-#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot_inter, tot_visits)
+        const float fr2 = p.far_ratio * p.far_ratio;
+        uint64_t tot_inter = 0, tot_visits = 0, tot_far_nodes = 0, tot_far_inter = 0;
+#pragma omp parallel for schedule(dynamic, 16) \
+    reduction(+ : tot_inter, tot_visits, tot_far_nodes, tot_far_inter)
         for (int64_t gi = 0; gi < (int64_t)groups.size(); ++gi) {
             const uint32_t gb = groups[gi].first, ge = groups[gi].second;
             const uint32_t s = sys_of[gb];
@@ -544,7 +630,13 @@ struct PhysState {
                     lo[a] = std::min(lo[a], rel[4ull * i + a]);
                     hi[a] = std::max(hi[a], rel[4ull * i + a]);
                 }
-            std::vector<uint32_t> frontier{offsets[lbits] + s}, next, cells, leaves;
+            float gc[3], hr[3];
+            for (int a = 0; a < 3; ++a) {
+                gc[a] = (lo[a] + hi[a]) * 0.5f;
+                hr[a] = (hi[a] - lo[a]) * 0.5f;
+            }
+            const float rg2 = fma2(hr[0], hr[0], fma2(hr[1], hr[1], hr[2] * hr[2]));
+            std::vector<uint32_t> frontier{offsets[lbits] + s}, next, cells, leaves, far;
             uint64_t tested = 0;
             for (int l = (int)lbits; !frontier.empty(); --l) {
                 next.clear();
@@ -555,7 +647,12 @@ struct PhysState {
                     for (int a = 0; a < 3; ++a) d[a] = std::max(std::max(lo[a] - c[a], c[a] - hi[a]), 0.0f);
                     float dist2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                     if (dist2 > node_crit2(nd, (uint32_t)l, s)) {
-                        cells.push_back(nd);
+                        bool is_far = false;
+                        if (fr2 > 0.0f) {
+                            const float D[3] = {c[0] - gc[0], c[1] - gc[1], c[2] - gc[2]};
+                            is_far = fr2 * fma2(D[0], D[0], fma2(D[1], D[1], D[2] * D[2])) > rg2;
+                        }
+                        (is_far ? far : cells).push_back(nd);
                     } else if (l == 0 || pend[nd] - pbeg[nd] <= p.bucket) {
                         leaves.push_back(nd);
                     } else {
@@ -564,11 +661,30 @@ struct PhysState {
                 }
                 frontier.swap(next);
             }
+            float fsum[kFarCoefs] = {};
+            if (!far.empty()) {
+                float part[kGroupMax][kFarCoefs] = {};
+                static const float kZeroQ[5] = {0, 0, 0, 0, 0};
+                for (size_t f = 0; f < far.size(); ++f) {
+                    float co[kFarCoefs];
+                    far_coefs(&cm[4ull * far[f]], quad_on ? &quad[5ull * far[f]] : kZeroQ, gc, co);
+                    for (int k = 0; k < kFarCoefs; ++k) part[f % kGroupMax][k] += co[k];
+                }
+                for (uint32_t o = kGroupMax / 2; o > 0; o >>= 1) {
+                    float nxt[kGroupMax][kFarCoefs];
+                    for (uint32_t l = 0; l < kGroupMax; ++l)
+                        for (int k = 0; k < kFarCoefs; ++k) nxt[l][k] = part[l][k] + part[l ^ o][k];
+                    std::memcpy(part, nxt, sizeof(part));
+                }
+                std::memcpy(fsum, part[0], sizeof(fsum));
+                tot_far_nodes += far.size();
+            }
             for (uint32_t ip = gb; ip < ge; ++ip) {
                 const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
                 BlockAcc A, B;
                 float t[3];
-                uint64_t inter = 0;
+                uint64_t inter = far.size();
+                tot_far_inter += far.size();
                 for (uint32_t nd : cells) {
                     const float* c = &cm[4ull * nd];
                     float dx = c[0] - px, dy = c[1] - py, dz = c[2] - pz;
@@ -592,6 +708,12 @@ struct PhysState {
                     }
                 B.finish(kahan);
                 float a3[3] = {A.s[0] + B.s[0], A.s[1] + B.s[1], A.s[2] + B.s[2]};
+                if (!far.empty()) {
+                    const float rho[3] = {px - gc[0], py - gc[1], pz - gc[2]};
+                    float fa[3];
+                    far_eval(fsum, rho, fa);
+                    for (int a = 0; a < 3; ++a) a3[a] = a3[a] + fa[a];
+                }
                 finish(ip, a3);
                 tot_inter += inter;
                 tot_visits += tested;
@@ -599,6 +721,8 @@ struct PhysState {
         }
         interactions = tot_inter;
         visits = tot_visits;
+        far_nodes = tot_far_nodes;
+        far_interactions = tot_far_inter;
     }
 
     // Kick-drift (BarnesHut.metal:189-194 without damping and type scale).
@@ -698,6 +822,8 @@ struct PhysState {
             for (uint32_t j = 0; j < n; ++j)
                 std::memcpy(&out->acc4[4ull * id[j]], &acc[4ull * j], 16);
         out->interactions = interactions;
+        out->far_nodes = far_nodes;
+        out->far_interactions = far_interactions;
         out->node_visits = visits;
         if (out->nodes) {
             for (uint64_t i = 0; i < capacity; ++i) {
@@ -723,6 +849,16 @@ struct PhysState {
 };
 
 }  // namespace
+
+extern "C" void oracle_far_expand(const astro_params* p, const float* cm4, const float* q5,
+                                  const float* gc3, const float* rho3, float* coefs19, float* acc3) {
+    PhysState st;
+    st.p = *p;
+    float co[PhysState::kFarCoefs];
+    st.far_coefs(cm4, q5, gc3, co);
+    if (coefs19) std::memcpy(coefs19, co, sizeof(co));
+    if (acc3) st.far_eval(co, rho3, acc3);
+}
 
 extern "C" int oracle_phys_run(const astro_params* p, PositionMass* pm, VelocityRadius* vr,
                                uint32_t n, const uint32_t* sys_sizes, uint32_t nsys, float dt,

@@ -51,6 +51,7 @@ def run_gpu(ag, params, pm, vr, ct=None, n_tree=None, dt=0.0, steps=1, sizes=Non
                    layer_sizes=sizes_, layer_offsets=offsets, layer_counts=counts,
                    nodes=sim.read_nodes(), acc4=sim.read_accel())
         out["interactions"], out["node_visits"] = sim.read_stats()
+        out["far_nodes"], out["far_interactions"] = sim.read_far_stats()
         out["pm"], out["vr"] = sim.download()
     return out
 
@@ -603,3 +604,67 @@ def test_delta_weight_bit_exact(ag, oracle, weight, form):
     assert_tree_equal(out, ref)
     assert np.array_equal(out["acc4"], ref["acc4"])
     assert out["interactions"] == ref["interactions"] and out["node_visits"] == ref["node_visits"]
+
+
+@pytest.mark.parametrize("ratio,form,walk,group_size,lbits", [
+    (0.2, 0, "group", 32, 10), (0.3, 1, "group", 32, 12), (0.15, 0, "group-monopole", 32, 21),
+    (0.25, 0, "group", 8, 10), (0.5, 1, "group", 1, 10), (0.4, 0, "group", 12, 6)])
+def test_far_nodes_bit_exact(ag, oracle, ratio, form, walk, group_size, lbits):
+    """Far nodes (one second-order expansion per group) in the exact form:
+    the accelerations, the integrated state and every counter equal the
+    CPU restatement's bit for bit."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=lbits, form=form, group_size=group_size,
+                          far_ratio=ratio, flags=WALKS[walk](L) | L.FLAG_IEEE_EXACT)
+    pm, vr = ic.plummer(16384, seed=1001)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    assert ref["far_nodes"] > 0
+    for k in ("interactions", "node_visits", "far_nodes", "far_interactions"):
+        assert out[k] == ref[k], k
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+def test_far_nodes_batched_bit_exact(ag, oracle):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    sizes = [1, 2, 31, 33, 1024, 5000, 64, 3, 4096, 777]
+    parts = [ic.plummer(s, seed=1004, a=0.5 + 0.1 * k, system=k) for k, s in enumerate(sizes)]
+    pm = np.concatenate([a for a, _ in parts])
+    vr = np.concatenate([b for _, b in parts])
+    p = ag.default_params(L.PRESET_PHYSICAL, far_ratio=0.25,
+                          flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2, sizes=sizes)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, sizes=sizes, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    assert out["far_nodes"] == ref["far_nodes"] > 0
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o)
+
+
+@pytest.mark.parametrize("ratio,form,warps,group_size,walk", [
+    (0.2, 0, 4, 32, "group"), (0.2, 1, 8, 32, "group"), (0.3, 0, 4, 12, "group"),
+    (0.15, 1, 4, 4, "group"), (0.2, 0, 8, 32, "group-monopole")])
+def test_far_nodes_fast_within_tolerance(ag, oracle, ratio, form, warps, group_size, walk):
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, flags=WALKS[walk](L), block_warps=warps,
+                          softening=0.005, lbits=14, form=form, group_size=group_size,
+                          far_ratio=ratio)
+    pm, vr = ic.disk_bulge(32768, seed=1002)
+    out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=1)
+    ref = oracle.phys_run(p, pm.copy(), vr.copy(), dt=5e-4, steps=1)
+    assert_tree_equal(out, ref)
+    ok, rel = acc_close(out["acc4"], ref["acc4"])
+    assert ok.all(), f"{(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
+    assert ref["far_nodes"] > 0
+    for k in ("interactions", "node_visits", "far_nodes", "far_interactions"):
+        assert out[k] == ref[k], k

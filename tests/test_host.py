@@ -30,6 +30,8 @@ def test_autotune_candidates_stay_in_range():
     assert set(autotune.candidates("block_warps", 1)) <= {2, 4, 8}
     assert autotune.candidates("sort_variant", 1) == list(range(1, 10))
     assert all(0 < w < 1 for w in autotune.candidates("open_delta_weight", 1))
+    assert all(0 < r <= 0.5 for r in autotune.candidates("far_ratio", 1))
+    assert set(autotune.ACCURACY_KNOBS) <= set(autotune.KNOBS)
     with pytest.raises(KeyError):
         autotune.candidates("theta", 1)
 
@@ -45,10 +47,11 @@ def test_tuned_file_feeds_bench_knobs(tmp_path, monkeypatch):
     import bench
 
     args = SimpleNamespace(workload="c2", form="plain", no_tuned=False, lbits=None, bucket=20,
-                           warps=None, group_size=None, sort_variant=None, delta_weight=None)
+                           warps=None, group_size=None, sort_variant=None, delta_weight=None,
+                           far_ratio=None)
     k, src = bench.knobs(args)
     assert k == {"lbits": 12, "bucket": 20, "block_warps": 8, "group_size": 16, "sort_variant": 3,
-                 "open_delta_weight": 1.0}
+                 "open_delta_weight": 1.0, "far_ratio": 0.0}
     assert src["bucket"] == "command line" and src["lbits"] == "autotuner"
     args.form = "precision"  # no entry: preset defaults
     k, src = bench.knobs(args)

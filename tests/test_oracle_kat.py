@@ -355,3 +355,113 @@ def test_delta_weight_zero_is_the_plain_opening_radius(oracle, native):
     w1 = oracle.phys_run(phys_params(), pm.copy(), vr.copy(), dt=0.0)
     assert np.array_equal(no_delta["acc4"], w0["acc4"])
     assert no_delta["interactions"] == w0["interactions"] < w1["interactions"]
+
+
+def _field64(D, m, Q, eps2):
+    """FP64 field of a node with quadrupole at displacement D (as the walk's terms)."""
+    r2 = D @ D + eps2
+    r = np.sqrt(r2)
+    qd = Q @ D
+    return m * D / r**3 + 2.5 * (D @ qd) * D / r**7 - qd / r**5
+
+
+def test_far_expansion_coefficients_are_the_taylor_series(oracle):
+    # The 19 coefficients of a far node are its field and that field's first
+    # and second derivatives at D = com - centre (checked against central
+    # differences of the FP64 field), and the expansion reproduces the field
+    # at an offset rho to third order in |rho| / |D|.
+    rng = np.random.default_rng(7)
+    xs = rng.uniform(-0.5, 0.5, (40, 3))
+    ms = rng.uniform(0.5, 1.5, 40)
+    com = (ms[:, None] * xs).sum(0) / ms.sum()
+    d = xs - com
+    Q = sum(m * (3 * np.outer(v, v) - v @ v * np.eye(3)) for v, m in zip(d, ms))
+    q5 = np.array([Q[0, 0], Q[1, 1], Q[0, 1], Q[0, 2], Q[1, 2]], np.float32)
+    Q = np.array([[q5[0], q5[2], q5[3]], [q5[2], q5[1], q5[4]], [q5[3], q5[4], -(q5[0] + q5[1])]],
+                 np.float64)
+    eps = 0.01
+    p = phys_params(softening=eps, g=2.0)
+    gc = np.array([0.3, -0.2, 0.1], np.float32)
+    cm4 = np.array([8.0, -5.0, 3.0, ms.sum()], np.float32)
+    D = cm4[:3].astype(np.float64) - gc
+    m = float(cm4[3])
+    co, _ = oracle.far_expand(p, cm4, q5, gc, np.zeros(3))
+    eps2 = float(np.float32(eps) * np.float32(eps))
+    a = _field64(D, m, Q, eps2)
+    h = 1e-4
+    J = np.zeros((3, 3))
+    H = np.zeros((3, 3, 3))
+    for j in range(3):
+        e = np.zeros(3)
+        e[j] = h
+        J[:, j] = (_field64(D + e, m, Q, eps2) - _field64(D - e, m, Q, eps2)) / (2 * h)
+        for k in range(3):
+            f = np.zeros(3)
+            f[k] = h
+            H[:, j, k] = (_field64(D + e + f, m, Q, eps2) - _field64(D + e - f, m, Q, eps2)
+                          - _field64(D - e + f, m, Q, eps2) + _field64(D - e - f, m, Q, eps2)) / (4 * h * h)
+    jj = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+    hh = [(0, 0, 0), (1, 1, 1), (2, 2, 2), (0, 0, 1), (0, 0, 2), (0, 1, 1), (1, 1, 2), (0, 2, 2),
+          (1, 2, 2), (0, 1, 2)]
+    want = np.concatenate([a, [J[i, j] for i, j in jj], [H[i, j, k] for i, j, k in hh]])
+    scale = np.concatenate([np.full(3, np.abs(a).max()), np.full(6, np.abs(J).max()),
+                            np.full(10, np.abs(H).max())])
+    assert np.all(np.abs(co - want) <= 1e-4 * scale), np.abs(co - want) / scale
+    # The expansion at offsets up to 10% of |D|: error ~ (|rho|/|D|)^3.
+    for frac in (0.02, 0.05, 0.1):
+        rho = rng.normal(size=3)
+        rho *= frac * np.linalg.norm(D) / np.linalg.norm(rho)
+        _, acc = oracle.far_expand(p, cm4, q5, gc, rho.astype(np.float32))
+        exact = 2.0 * _field64(D - rho.astype(np.float32), m, Q, eps2)
+        rel = np.linalg.norm(acc - exact) / np.linalg.norm(exact)
+        assert rel < 2.0 * frac**3 + 1e-5, (frac, rel)
+
+
+def test_far_nodes_keep_the_walk_and_the_accuracy(oracle, native):
+    # far_ratio changes how accepted nodes are summed, never which: the
+    # interaction and visit counts stay, the far counts grow with the ratio,
+    # and the accelerations stay within the expansion's third-order error
+    # (the error against the FP64 direct sum barely moves).
+    from astro_gb300 import ic
+
+    pm, vr = ic.plummer(16384, seed=1001)
+    samples = np.random.default_rng(0).choice(len(pm), 256, replace=False)
+    ref = oracle.direct_accel(pm, samples, g=1.0, eps=0.01)
+    runs = {r: oracle.phys_run(phys_params(lbits=10, far_ratio=r), pm.copy(), vr.copy(), dt=0.0)
+            for r in (0.0, 0.1, 0.2)}
+    base = runs[0.0]
+    assert base["far_nodes"] == 0 and base["far_interactions"] == 0
+    errs = {}
+    for r, out in runs.items():
+        assert out["interactions"] == base["interactions"]
+        assert out["node_visits"] == base["node_visits"]
+        acc = out["acc4"].reshape(-1, 4)[samples, :3].astype(np.float64)
+        errs[r] = np.median(np.linalg.norm(acc - ref, axis=1) / np.linalg.norm(ref, axis=1))
+    assert 0 < runs[0.1]["far_interactions"] < runs[0.2]["far_interactions"] < base["interactions"]
+    assert runs[0.1]["far_nodes"] < runs[0.1]["far_interactions"]
+    a0 = base["acc4"].reshape(-1, 4)[:, :3].astype(np.float64)
+    a1 = runs[0.1]["acc4"].reshape(-1, 4)[:, :3].astype(np.float64)
+    rel = np.linalg.norm(a1 - a0, axis=1) / np.linalg.norm(a0, axis=1)
+    assert np.median(rel) < 1e-4 and rel.max() < 1e-2
+    assert errs[0.1] < 1.05 * errs[0.0] and errs[0.2] < 1.2 * errs[0.0]
+
+
+def test_far_ratio_one_particle_groups_and_systems(oracle, native):
+    # Groups of one particle (box of zero size): every accepted node is far,
+    # in every system of a batch.
+    from astro_gb300 import ic
+
+    sizes = [1, 2, 300, 1000]
+    parts = [ic.plummer(s, seed=1004, system=k) for k, s in enumerate(sizes)]
+    pm = np.concatenate([a for a, _ in parts])
+    vr = np.concatenate([b for _, b in parts])
+    near = oracle.phys_run(phys_params(group_size=1), pm.copy(), vr.copy(), sizes=sizes, dt=0.0)
+    far = oracle.phys_run(phys_params(group_size=1, far_ratio=0.5), pm.copy(), vr.copy(),
+                          sizes=sizes, dt=0.0)
+    assert far["interactions"] == near["interactions"]
+    assert far["far_nodes"] == far["far_interactions"] > 0
+    a0 = near["acc4"].reshape(-1, 4)[:, :3].astype(np.float64)
+    a1 = far["acc4"].reshape(-1, 4)[:, :3].astype(np.float64)
+    # rho = 0 for a single particle: the expansion is the node's field itself.
+    rel = np.linalg.norm(a1 - a0, axis=1) / np.maximum(np.linalg.norm(a0, axis=1), 1e-30)
+    assert rel.max() < 1e-5
