@@ -228,7 +228,9 @@ constexpr int kTopoTile = kTopoThreads * kTopoItems;
 // look-back across tiles. Each start writes the node's first particle and,
 // above layer 0, its first child (the node starting at i one layer down).
 // This yields the runs of markUniques/scatterUniques (Octree.metal:282-318)
-// for all layers without re-sorting or re-scanning per layer.
+// for all layers without re-sorting or re-scanning per layer. Each node
+// below the top layer also gets its parent: the node one layer up that
+// holds its first particle (the bottom-up aggregation climbs these links).
 __global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_off[ASTRO_MAX_LAYERS];
@@ -299,16 +301,26 @@ __global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
     for (int k = 0; k < kTopoItems; ++k) {
         const uint32_t i = (uint32_t)(warp_base + 32ull * k + lane);
         uint32_t idx_below = 0;
+        uint32_t pending = kNoParent;  // this lane's node one layer down, parent not yet written
         for (int l = 0; l <= lbits; ++l) {
             const uint32_t b = __ballot_sync(kFullMask, lev[k] >= l);
-            if (b == 0) break;
             const uint32_t base_l = __shfl_sync(kFullMask, running, l);
+            // Starts of layer l before particle i.
+            const uint32_t rank = base_l + __popc(b & lt);
+            if (pending != kNoParent) {
+                // The parent holds i: the layer-l node starting at i, else the
+                // last one starting before it.
+                a.parent[pending] = s_off[l] + (lev[k] >= l ? rank : rank - 1u);
+                pending = kNoParent;
+            }
+            if (b == 0) break;
             if (lev[k] >= l) {
-                const uint32_t idx = base_l + __popc(b & lt);
-                const uint32_t node = s_off[l] + idx;
+                const uint32_t node = s_off[l] + rank;
                 a.pbeg[node] = i;
                 if (l > 0) a.cbeg[node] = s_off[l - 1] + idx_below;
-                idx_below = idx;
+                idx_below = rank;
+                if (l < lbits) pending = node;
+                else a.parent[node] = kNoParent;
             }
             if ((int)lane == l) running += __popc(b);
         }
@@ -379,10 +391,7 @@ __device__ __forceinline__ void emit_group(const AggArgs& a, uint32_t b, uint32_
 // kMode 2 (PHYSICAL precision): FP64 sums of m and m*x over the FP32
 //   positions relative to the system origin.
 template <int kMode>
-__global__ void aggregate_leaf_kernel(AggArgs a) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t u0 = a.layer_count[0];
-    if (j >= u0) return;
+__device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j, uint32_t u0) {
     const uint32_t pb = a.pbeg[j];
     const uint32_t pe = (j + 1 < u0) ? a.pbeg[j + 1] : a.n;
     const uint64_t key = a.sorted_keys[pb];
@@ -463,12 +472,21 @@ __global__ void aggregate_leaf_kernel(AggArgs a) {
 // order with the same roundings as a sequential loop.
 // kMode 0 sums child centre of mass times child mass (the reference's
 // formula); kModes 1 and 2 add the children's raw sums.
+// Children are read through L2 (ld.global.cg): the climbing kernel below
+// reads records that other blocks wrote in the same launch.
+__device__ __forceinline__ float4 ld_l2(const float4* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_l2(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ uint4 ld_l2(const uint4* p) { return __ldcg(p); }
+__device__ __forceinline__ double4 ld_l2(const double4* p) {
+    const double2 lo = __ldcg(reinterpret_cast<const double2*>(p));
+    const double2 hi = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+    return make_double4(lo.x, lo.y, hi.x, hi.y);
+}
+
 template <int kMode>
-__global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint32_t l, uint32_t off,
-                                                                 uint32_t off_below) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t u = a.layer_count[l];
-    if (j >= u) return;
+__device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32_t l, uint32_t j,
+                                                        uint32_t u) {
+    const uint32_t off = a.offset[l], off_below = a.offset[l - 1];
     const uint32_t node = off + j;
     const uint32_t cb = a.node_cbeg[node];
     const uint32_t ce = (j + 1 < u) ? a.node_cbeg[node + 1] : off_below + a.layer_count[l - 1];
@@ -484,7 +502,7 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
     if (need_ccm) {
 #pragma unroll
         for (uint32_t k = 0; k < 8; ++k)
-            ccm[k] = k < nch ? a.node_cm[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+            ccm[k] = k < nch ? ld_l2(a.node_cm + cb + k) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (kMode == 0) {
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
@@ -506,15 +524,15 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
         // so the sums, the centre of mass and the moments equal the child's;
         // copying them is what the arithmetic below would produce.
         if (kMode == 1)
-            reinterpret_cast<float4*>(a.node_sum)[node] = reinterpret_cast<const float4*>(a.node_sum)[cb];
+            reinterpret_cast<float4*>(a.node_sum)[node] = ld_l2(reinterpret_cast<const float4*>(a.node_sum) + cb);
         else
-            reinterpret_cast<double4*>(a.node_sum)[node] = reinterpret_cast<const double4*>(a.node_sum)[cb];
-        cm = need_ccm ? ccm[0] : a.node_cm[cb];
+            reinterpret_cast<double4*>(a.node_sum)[node] = ld_l2(reinterpret_cast<const double4*>(a.node_sum) + cb);
+        cm = need_ccm ? ccm[0] : ld_l2(a.node_cm + cb);
     } else if (kMode == 1) {
         const float4* sum = reinterpret_cast<const float4*>(a.node_sum);
         float4 cs[8];
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? sum[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? ld_l2(sum + cb + k) : make_float4(0.f, 0.f, 0.f, 0.f);
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
         for (uint32_t k = 0; k < 8; ++k) {
@@ -531,7 +549,7 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
         const double4* sum = reinterpret_cast<const double4*>(a.node_sum);
         double4 cs[8];
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? sum[cb + k] : make_double4(0.0, 0.0, 0.0, 0.0);
+        for (uint32_t k = 0; k < 8; ++k) cs[k] = k < nch ? ld_l2(sum + cb + k) : make_double4(0.0, 0.0, 0.0, 0.0);
         double m = 0, sx = 0, sy = 0, sz = 0;
 #pragma unroll
         for (uint32_t k = 0; k < 8; ++k) {
@@ -549,15 +567,15 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
     a.node_rng[node] = make_uint4(cb, ce, pb, pe);
     if (kMode != 0) {
         if (a.want_quad && nch == 1) {
-            a.node_q[node] = a.node_q[cb];
-            a.node_qyz[node] = a.node_qyz[cb];
+            a.node_q[node] = ld_l2(a.node_q + cb);
+            a.node_qyz[node] = ld_l2(a.node_qyz + cb);
         } else if (a.want_quad) {
             float4 qc[8];
             float qyz[8];
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
-                qc[k] = k < nch ? a.node_q[cb + k] : make_float4(0.f, 0.f, 0.f, 0.f);
-                qyz[k] = k < nch ? a.node_qyz[cb + k] : 0.f;
+                qc[k] = k < nch ? ld_l2(a.node_q + cb + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+                qyz[k] = k < nch ? ld_l2(a.node_qyz + cb + k) : 0.f;
             }
             float q[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -584,8 +602,8 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
             uint2 cr[8];
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
-                const uint4* rng = a.node_rng + cb + k;
-                cr[k] = k < nch ? make_uint2(__ldg(&rng->z), __ldg(&rng->w)) : make_uint2(0u, 0u);
+                const uint4 rng = k < nch ? ld_l2(a.node_rng + cb + k) : make_uint4(0u, 0u, 0u, 0u);
+                cr[k] = make_uint2(rng.z, rng.w);
             }
             uint32_t gb = 0, ge = 0;
 #pragma unroll
@@ -612,6 +630,61 @@ __global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint
         } else if (l == a.lbits) {
             emit_group(a, pb, pe);
         }
+    }
+}
+
+// Bottom-up aggregation. Layers of at least kClimbMinNodes nodes (capacity)
+// run one launch each, a thread per node with coalesced records; the rest
+// of the tree runs in one launch that climbs: a thread per node of the
+// first small layer aggregates its node, then makes the records visible
+// (fence) and counts itself in at the parent; the thread that brings the
+// parent's count to its number of children aggregates the parent (reading
+// the children through L2) and climbs on; the others stop. Every node is
+// aggregated once, after all its children, with the arithmetic of the
+// per-node functions above; no thread waits on another. The small top
+// layers thus cost one launch instead of one each.
+constexpr uint32_t kClimbMinNodes = 32768;
+template <int kMode>
+__global__ __launch_bounds__(128) void aggregate_leaf_kernel(AggArgs a) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u0 = a.layer_count[0];
+    if (j < u0) aggregate_leaf_node<kMode>(a, j, u0);
+}
+
+template <int kMode>
+__global__ __launch_bounds__(128) void aggregate_internal_kernel(AggArgs a, uint32_t l) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u = a.layer_count[l];
+    if (j < u) aggregate_internal_node<kMode>(a, l, j, u);
+}
+
+// Layers l0 and up in one launch: one thread per node of layer l0.
+template <int kMode>
+__global__ __launch_bounds__(128) void aggregate_tree_kernel(AggArgs a, uint32_t l0) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u0 = a.layer_count[l0];
+    if (j >= u0) return;
+    if (l0 == 0) aggregate_leaf_node<kMode>(a, j, u0);
+    else aggregate_internal_node<kMode>(a, l0, j, u0);
+    uint32_t node = a.offset[l0] + j;
+    for (uint32_t l = l0 + 1; l <= a.lbits; ++l) {
+        const uint32_t p = a.parent[node];
+        if (p == kNoParent) return;
+        const uint32_t u = a.layer_count[l];
+        const uint32_t jp = p - a.offset[l];
+        if (jp >= u) {
+            atomicOr(a.err, kErrBadLayer);
+            return;
+        }
+        const uint32_t cb = a.node_cbeg[p];
+        const uint32_t ce = (jp + 1 < u) ? a.node_cbeg[p + 1] : a.offset[l - 1] + a.layer_count[l - 1];
+        if (ce - cb > 1u) {
+            __threadfence();
+            if (atomicAdd(&a.arrive[p], 1u) != ce - cb - 1u) return;
+            __threadfence();
+        }
+        aggregate_internal_node<kMode>(a, l, jp, u);
+        node = p;
     }
 }
 
@@ -956,20 +1029,31 @@ cudaError_t launch_topology(const TopoArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+uint32_t climb_first_layer(const LayerTable& t) {
+    uint32_t l0 = 0;
+    while (l0 + 1 < t.n_layers && t.size[l0] >= kClimbMinNodes) ++l0;
+    return l0;
+}
+
 cudaError_t launch_aggregate(int mode, const AggArgs& a, const LayerTable& t, cudaStream_t st) {
     const uint32_t t0 = 128;
-    if (mode == 0) aggregate_leaf_kernel<0><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
-    else if (mode == 1) aggregate_leaf_kernel<1><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
-    else aggregate_leaf_kernel<2><<<blocks_for(t.size[0], t0), t0, 0, st>>>(a);
-    for (uint32_t l = 1; l < t.n_layers; ++l) {
+    const uint32_t l0 = climb_first_layer(t);
+    for (uint32_t l = 0; l < l0; ++l) {
         const uint32_t g = blocks_for(t.size[l], t0);
-        if (mode == 0)
-            aggregate_internal_kernel<0><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
-        else if (mode == 1)
-            aggregate_internal_kernel<1><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
-        else
-            aggregate_internal_kernel<2><<<g, t0, 0, st>>>(a, l, t.offset[l], t.offset[l - 1]);
+        if (l == 0) {
+            if (mode == 0) aggregate_leaf_kernel<0><<<g, t0, 0, st>>>(a);
+            else if (mode == 1) aggregate_leaf_kernel<1><<<g, t0, 0, st>>>(a);
+            else aggregate_leaf_kernel<2><<<g, t0, 0, st>>>(a);
+        } else {
+            if (mode == 0) aggregate_internal_kernel<0><<<g, t0, 0, st>>>(a, l);
+            else if (mode == 1) aggregate_internal_kernel<1><<<g, t0, 0, st>>>(a, l);
+            else aggregate_internal_kernel<2><<<g, t0, 0, st>>>(a, l);
+        }
     }
+    const uint32_t g = blocks_for(t.size[l0], t0);
+    if (mode == 0) aggregate_tree_kernel<0><<<g, t0, 0, st>>>(a, l0);
+    else if (mode == 1) aggregate_tree_kernel<1><<<g, t0, 0, st>>>(a, l0);
+    else aggregate_tree_kernel<2><<<g, t0, 0, st>>>(a, l0);
     return cudaGetLastError();
 }
 

@@ -16,6 +16,7 @@ struct TopoArgs {
     uint32_t offset[ASTRO_MAX_LAYERS];
     uint32_t* pbeg;
     uint32_t* cbeg;
+    uint32_t* parent;    // per node: the node one layer up holding it (kNoParent at the top)
     uint32_t* layer_count;
     uint32_t* lookback;  // [ntiles][32] status words
     uint32_t* tile_counter;
@@ -30,7 +31,10 @@ struct AggArgs {
     const SysInfo* sys;
     const uint32_t* pbeg;
     const uint32_t* node_cbeg;
+    const uint32_t* parent;    // per node: its parent (kNoParent at the top layer)
+    uint32_t* arrive;          // per internal node: children aggregated so far (zeroed per build)
     const uint32_t* layer_count;
+    uint32_t offset[ASTRO_MAX_LAYERS];  // first node of each layer
     float4* node_cm;
     uint4* node_rng;
     uint64_t* node_key;
@@ -52,6 +56,7 @@ struct AggArgs {
 };
 
 constexpr uint32_t kGroupSize = 32;  // largest group of the group walk (one warp)
+constexpr uint32_t kNoParent = 0xFFFFFFFFu;
 
 struct DirectArgs {
     const float4* pos;
@@ -129,6 +134,8 @@ cudaError_t launch_reorder(bool prec, const uint32_t* perm, const float4* pos_a,
                            uint32_t* id_b, double* x_b, uint32_t n, cudaStream_t st);
 uint32_t topology_tiles(uint32_t n);
 cudaError_t launch_topology(const TopoArgs& a, cudaStream_t st);
+// First layer the bottom-up aggregation climbs from (below it: one launch per layer).
+uint32_t climb_first_layer(const LayerTable& t);
 cudaError_t launch_aggregate(int mode, const AggArgs& a, const LayerTable& t, cudaStream_t st);
 cudaError_t launch_integrate_ref(float4* pos, float4* vel, const float4* acc, const uint32_t* types,
                                  uint32_t n, float dt, const astro_params& p, cudaStream_t st);

@@ -128,6 +128,8 @@ int ensure_tree(astro_ctx* ctx, uint64_t capacity) {
     ctx->node_sum = nullptr;
     dev_free(ctx->node_pbeg);
     dev_free(ctx->node_cbeg);
+    dev_free(ctx->node_parent);
+    dev_free(ctx->node_arrive);
     dev_free(ctx->node_crit2);
     dev_free(ctx->node_q);
     dev_free(ctx->node_qyz);
@@ -142,6 +144,8 @@ int ensure_tree(astro_ctx* ctx, uint64_t capacity) {
     CK(cudaMalloc(&ctx->node_sum, cap * 32));  // room for double4 sums
     CK(dev_alloc(&ctx->node_pbeg, cap + 1));
     CK(dev_alloc(&ctx->node_cbeg, cap + 1));
+    CK(dev_alloc(&ctx->node_parent, cap));
+    CK(dev_alloc(&ctx->node_arrive, cap));
     ctx->tree_capacity = cap;
     return ASTRO_OK;
 }
@@ -262,6 +266,7 @@ int stage_build(astro_ctx* ctx) {
     for (uint32_t l = 0; l <= ctx->lbits; ++l) t.offset[l] = ctx->layers.offset[l];
     t.pbeg = ctx->node_pbeg;
     t.cbeg = ctx->node_cbeg;
+    t.parent = ctx->node_parent;
     t.layer_count = ctx->layer_count;
     t.lookback = ctx->topo_lookback;
     t.tile_counter = ctx->counters;
@@ -276,7 +281,10 @@ int stage_build(astro_ctx* ctx) {
     a.sys = ctx->sys;
     a.pbeg = ctx->node_pbeg;
     a.node_cbeg = ctx->node_cbeg;
+    a.parent = ctx->node_parent;
+    a.arrive = ctx->node_arrive;
     a.layer_count = ctx->layer_count;
+    for (uint32_t l = 0; l <= ctx->lbits; ++l) a.offset[l] = ctx->layers.offset[l];
     a.node_cm = ctx->node_cm;
     a.node_rng = ctx->node_rng;
     a.node_key = ctx->node_key;
@@ -295,6 +303,13 @@ int stage_build(astro_ctx* ctx) {
     a.group_size = ctx->p.group_size ? ctx->p.group_size : astro::kGroupSize;
     a.err = ctx->err;
     CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
+    const uint32_t l0 = astro::climb_first_layer(ctx->layers);
+    if (l0 < ctx->lbits) {
+        // Arrival counters of the layers the aggregation climbs into.
+        const uint64_t first = ctx->layers.offset[l0 + 1];
+        const uint64_t end = (uint64_t)ctx->layers.offset[ctx->lbits] + ctx->layers.size[ctx->lbits];
+        CK(cudaMemsetAsync(ctx->node_arrive + first, 0, (end - first) * sizeof(uint32_t), st));
+    }
     const int mode = !is_phys(ctx) ? 0 : (is_prec(ctx) ? 2 : 1);
     CK(astro::launch_aggregate(mode, a, ctx->layers, st));
     ctx->tree_valid = true;
@@ -598,6 +613,8 @@ int astro_destroy(astro_ctx* ctx) {
     if (ctx->node_sum) cudaFree(ctx->node_sum);
     dev_free(ctx->node_pbeg);
     dev_free(ctx->node_cbeg);
+    dev_free(ctx->node_parent);
+    dev_free(ctx->node_arrive);
     dev_free(ctx->node_crit2);
     dev_free(ctx->node_q);
     dev_free(ctx->node_qyz);

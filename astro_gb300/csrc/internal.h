@@ -119,6 +119,8 @@ struct astro_ctx {
     void* node_sum = nullptr;         // float4 or double4 raw sums (S, M)
     uint32_t* node_pbeg = nullptr;
     uint32_t* node_cbeg = nullptr;
+    uint32_t* node_parent = nullptr;
+    uint32_t* node_arrive = nullptr;
     float* node_crit2 = nullptr;      // opening radius^2 per node
     float4* node_q = nullptr;         // quadrupole Qxx, Qyy, Qxy, Qxz
     float* node_qyz = nullptr;        // quadrupole Qyz

@@ -593,10 +593,6 @@ struct CellSlot<false> {
 #ifndef ASTRO_GROUP_WARPS_PER_SM
 #define ASTRO_GROUP_WARPS_PER_SM 24
 #endif
-// Far-node loop with the next node's record loaded ahead (1) or not (0).
-#ifndef ASTRO_FAR_PREFETCH
-#define ASTRO_FAR_PREFETCH 0
-#endif
 #if ASTRO_GROUP_WARPS_PER_SM > 0
 #define ASTRO_GROUP_BOUNDS(w) __launch_bounds__((w) * 32, ASTRO_GROUP_WARPS_PER_SM / (w))
 #else
@@ -947,45 +943,6 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             float fc[kFarCoefs];
 #pragma unroll
             for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
-#if ASTRO_FAR_PREFETCH
-            // The next far node's record is loaded before this one is
-            // expanded, so the dependent loads (list entry, then record)
-            // overlap the arithmetic.
-            uint32_t f = lane;
-            uint32_t nd_next = f + 32u < far_total ? far_list[f + 32u] : 0u;
-            float4 c = make_float4(0.f, 0.f, 0.f, 0.f), q = c;
-            float qyz = 0.f;
-            if (f < far_total) {
-                const uint32_t nd = far_list[f];
-                c = __ldg(&a.node_cm[nd]);
-                if constexpr (kQuad) {
-                    q = __ldg(&a.node_q[nd]);
-                    qyz = __ldg(&a.node_qyz[nd]);
-                }
-            }
-            for (; f < far_total; f += 32u) {
-                const bool more = f + 32u < far_total;
-                float4 cn = make_float4(0.f, 0.f, 0.f, 0.f), qn = cn;
-                float qyzn = 0.f;
-                uint32_t nd_after = 0u;
-                if (more) {
-                    cn = __ldg(&a.node_cm[nd_next]);
-                    if constexpr (kQuad) {
-                        qn = __ldg(&a.node_q[nd_next]);
-                        qyzn = __ldg(&a.node_qyz[nd_next]);
-                    }
-                    if (f + 64u < far_total) nd_after = far_list[f + 64u];
-                }
-                if constexpr (kQuad)
-                    far_coefs<kExact, true>(c, q, qyz, -(q.x + q.y), gcx, gcy, gcz, eps2, fc);
-                else
-                    far_coefs<kExact, false>(c, q, 0.f, 0.f, gcx, gcy, gcz, eps2, fc);
-                c = cn;
-                q = qn;
-                qyz = qyzn;
-                nd_next = nd_after;
-            }
-#else
             for (uint32_t f = lane; f < far_total; f += 32u) {
                 const uint32_t nd = far_list[f];
                 const float4 c = __ldg(&a.node_cm[nd]);
@@ -998,7 +955,6 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
                                              gcz, eps2, fc);
                 }
             }
-#endif
 #pragma unroll
             for (int k = 0; k < kFarCoefs; ++k) {
                 float v = fc[k];

@@ -668,3 +668,22 @@ def test_far_nodes_fast_within_tolerance(ag, oracle, ratio, form, warps, group_s
     assert ref["far_nodes"] > 0
     for k in ("interactions", "node_visits", "far_nodes", "far_interactions"):
         assert out[k] == ref[k], k
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_build_per_layer_and_climbing_bit_exact(ag, oracle, form):
+    """131,072 particles at lbits 12: the large bottom layers are aggregated
+    one launch each and the small top layers in one climbing launch; the
+    tree, the forces and the state must equal the restatement's."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=12, form=form, softening=0.005,
+                          far_ratio=0.2, flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    pm, vr = ic.disk_bulge(131072, seed=1002)
+    out = run_gpu(ag, p, pm, vr, dt=5e-4, steps=1)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, dt=5e-4, steps=1)
+    assert_tree_equal(out, ref)
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
