@@ -1,5 +1,9 @@
 """Autotuner of the Barnes-Hut step's launch knobs on the current GPU.
 
+The search runs in the library (astro_autotune / astro_autotune_ex,
+astro_gb300/csrc/tune.cu) on a context's own particles; this module drives
+it over the benchmark workloads and collects the results file.
+
 The knobs are fields of astro_params that change speed, not physics:
 
   block_warps   traversal block size (warps per block: 4 or 8)
@@ -65,6 +69,8 @@ FORMS = {"plain": L.FORM_PLAIN, "precision": L.FORM_PRECISION}
 
 
 def candidates(knob: str, n: int) -> list[int]:
+    """The values the library's search tries for a knob (n: the largest
+    system's particle count)."""
     if knob == "lbits":
         # From about 8 particles per finest cell down to single occupancy.
         lo = max(3, int(np.ceil(np.log2(max(n, 8) / 8) / 3)))
@@ -84,135 +90,32 @@ def candidates(knob: str, n: int) -> list[int]:
     raise KeyError(knob)
 
 
-class Trial:
-    """One workload on the device: particles, FP64 reference accelerations on
-    sampled particles, and timing of parameter settings."""
-
-    def __init__(self, workload: str, form: int, samples: int = 1024, seed: int = 5):
-        self.w = WORKLOADS[workload]
-        self.form = form
-        self.pm, self.vr, self.sizes = self.w.make()
-        self.n = len(self.pm)
-        self.nsys = len(self.sizes) if self.sizes else 1
-        rng = np.random.default_rng(seed)
-        self.samples = np.sort(rng.choice(self.n, size=min(samples, self.n), replace=False)).astype(
-            np.uint32)
-        self.direct = None
-
-    def params(self, knobs: dict) -> L.Params:
-        return default_params(L.PRESET_PHYSICAL, form=self.form, **self.w.physics, **knobs)
-
-    def run(self, knobs: dict, steps: int, warmup: int = 3) -> dict:
-        import torch
-
-        sim = Simulation(self.params(knobs), max_n=self.n, max_systems=self.nsys)
-        try:
-            if self.sizes:
-                sim.upload_systems(self.pm, self.vr, self.sizes)
-            else:
-                sim.upload(self.pm, self.vr)
-            sim.draw(0.0, warmup)
-            sim.synchronize()
-            if self.direct is None:
-                self.direct = sim.direct_accel_f64(self.samples)
-            stream = torch.cuda.ExternalStream(sim.stream)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-            with torch.cuda.stream(stream):
-                ev[0].record(stream)
-                sim.draw(0.0, steps)
-                ev[1].record(stream)
-            sim.synchronize()
-            step_ms = ev[0].elapsed_time(ev[1]) / steps
-            # The sort stage alone (median of three eager stage sequences).
-            sort_ms = []
-            for _ in range(3):
-                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                with torch.cuda.stream(stream):
-                    sim.generate_morton_codes()
-                    e[0].record(stream)
-                    sim.sort()
-                    e[1].record(stream)
-                    sim.build_tree()
-                    sim.barnes_hut()
-                    sim.update_spheres(0.0)
-                sim.synchronize()
-                sort_ms.append(e[0].elapsed_time(e[1]))
-            sim.generate_morton_codes()
-            sim.sort()
-            sim.build_tree()
-            sim.barnes_hut()
-            acc = sim.read_accel()
-            sim.update_spheres(0.0)
-            err = np.linalg.norm(acc[self.samples, :3] - self.direct, axis=1) / np.linalg.norm(
-                self.direct, axis=1)
-        finally:
-            sim.close()
-        return {"knobs": dict(knobs), "ms": step_ms, "sort_ms": float(np.median(sort_ms)),
-                "median_error": float(np.median(err))}
-
-
-def tune(workload: str, form: str, target: float = 1e-3, steps: int | None = None,
+def tune(workload: str, form: str, target: float = 1e-3, samples: int = 1024,
          log=print) -> dict:
-    t = Trial(workload, FORMS[form])
-    start = {"lbits": t.w.lbits, "bucket": 16, "group_size": 32, "block_warps": 4,
-             "sort_variant": 0, "far_ratio": 0.0, "open_delta_weight": 1.0}
-    if not steps:
-        # About 60 ms of timed steps per trial.
-        steps = int(np.clip(60.0 / t.run(start, 3)["ms"], 3, 60))
-    best = t.run(start, steps)
-    trials = [best]
-    bound = max(target, 1.02 * best["median_error"])
-    # Accuracy knobs: within 0.8 x the target, or no more than 2% above the
-    # starting error where that error is already set by theta (above 0.8 x).
-    acc_bound = max(0.8 * target, 1.02 * best["median_error"])
-    log(f"{workload}/{form} start {start}: {best['ms']:.3f} ms, error {best['median_error']:.3g}")
-    nmax = max(t.sizes) if t.sizes else t.n
-
-    def sweep(knob, limit):
-        nonlocal best
-        for v in candidates(knob, nmax):
-            if knob == "lbits" and 3 * v + (t.nsys - 1).bit_length() > 64:
-                continue
-            if v == best["knobs"][knob]:
-                continue
-            r = t.run(dict(best["knobs"], **{knob: v}), steps)
-            trials.append(r)
-            key = "sort_ms" if knob == "sort_variant" else "ms"
-            better = r[key] < best[key] and r["median_error"] <= limit
-            log(f"  {knob}={v}: {r['ms']:.3f} ms (sort {r['sort_ms']:.3f}), error "
-                f"{r['median_error']:.3g}{'  <- best' if better else ''}")
-            if better:
-                best = r
-
-    perf = [k for k in KNOBS if k not in ACCURACY_KNOBS]
-    for knob in perf:
-        sweep(knob, bound)
-    # The accuracy knobs share one error budget: every (open_delta_weight,
-    # far_ratio) pair, far_ratio rising until the error leaves the bound.
-    base = dict(best["knobs"])
-    for w in [1.0] + candidates("open_delta_weight", nmax):
-        for f in [0.0] + candidates("far_ratio", nmax):
-            k = dict(base, open_delta_weight=w, far_ratio=f)
-            if k == best["knobs"]:
-                continue
-            r = t.run(k, steps)
-            trials.append(r)
-            ok = r["median_error"] <= acc_bound
-            better = ok and r["ms"] < best["ms"]
-            log(f"  open_delta_weight={w}, far_ratio={f}: {r['ms']:.3f} ms, error "
-                f"{r['median_error']:.3g}{'  <- best' if better else ''}")
-            if better:
-                best = r
-            if not ok:
-                break
-    # The tree and launch knobs again, around the chosen accuracy knobs
-    # (group boxes now also decide which nodes are far: the accuracy bound).
-    for knob in ("lbits", "bucket", "group_size", "block_warps"):
-        sweep(knob, acc_bound)
-    return {"workload": workload, "form": form, "n": t.n, "knobs": best["knobs"],
-            "ms": best["ms"], "sort_ms": best["sort_ms"], "median_error": best["median_error"],
-            "error_bound": bound, "accuracy_knob_bound": acc_bound, "steps_timed": steps,
-            "trials": trials}
+    """Tune one workload with the library's native search (astro_autotune_ex)
+    from the preset's defaults at the workload's starting depth."""
+    w = WORKLOADS[workload]
+    pm, vr, sizes = w.make()
+    params = default_params(L.PRESET_PHYSICAL, form=FORMS[form], lbits=w.lbits, **w.physics)
+    sim = Simulation(params, max_n=len(pm), max_systems=len(sizes) if sizes else 1)
+    try:
+        if sizes:
+            sim.upload_systems(pm, vr, sizes)
+        else:
+            sim.upload(pm, vr)
+        res = sim.autotune(target=target, samples=samples)
+    finally:
+        sim.close()
+    start = res["trials"][0]
+    log(f"{workload}/{form} start {start['knobs']}: {start['ms']:.3f} ms, error "
+        f"{start['median_error']:.3g}")
+    best = start
+    for t in res["trials"][1:]:
+        if t["knobs"] == res["knobs"] and t["ms"] == res["ms"]:
+            best = t
+        log(f"  {t['knobs']}: {t['ms']:.3f} ms (sort {t['sort_ms']:.3f}), error "
+            f"{t['median_error']:.3g}{'  <- chosen' if t is best else ''}")
+    return {"workload": workload, "form": form, **res}
 
 
 def load(path: Path | None = None) -> dict:
@@ -241,7 +144,7 @@ def main(argv=None) -> int:
             out = {"device": torch.cuda.get_device_name(),
                    "sms": torch.cuda.get_device_properties(0).multi_processor_count,
                    "when": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
-                   "method": "coordinate descent over " + ", ".join(KNOBS) +
+                   "method": "astro_autotune_ex: coordinate descent over " + ", ".join(KNOBS) +
                              "; step time by CUDA events over graph-replayed steps (dt = 0)",
                    "results": results}
             args.out.write_text(json.dumps(out, indent=1) + "\n")

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 SOURCES = ["sort.cu", "sort_noalloc.cu", "build.cu", "traverse.cu", "splat.cu", "context.cu",
-           "ic.cpp"]
+           "tune.cu", "ic.cpp"]
 
 
 def nvcc() -> str:

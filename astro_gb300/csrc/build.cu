@@ -1,4 +1,4 @@
-// Encode, bounding box, tree topology and per-layer aggregation kernels.
+// Encode, bounding box, tree topology and aggregation kernels.
 //
 // Reference stages replaced here (Astro/Renderer.swift:505-533,714-755):
 //   generateMortonCodes + fillIndices (MortonCode.metal:26-52, Octree.metal:39-51)
@@ -7,8 +7,9 @@
 //   aggregateLeafNodes / aggregateNodes (Octree.metal:53-202)
 // The reference finds the runs of every layer with one sort + scan + scatter
 // per layer over all N entries. Here a single pass over the sorted keys finds
-// the node starts of all layers at once (topology_kernel), and one kernel
-// per layer aggregates mass and centre of mass.
+// the node starts of all layers at once (topology_kernel); the large layers
+// are aggregated one launch each and the small top layers in one climbing
+// launch (aggregate_tree_kernel).
 #include <algorithm>
 
 #include "build_kernels.cuh"
@@ -465,7 +466,7 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
     }
 }
 
-// aggregateNodes (Octree.metal:120-202), one thread per node of layer l.
+// aggregateNodes (Octree.metal:120-202) for node j of layer l (one thread).
 // Children are the contiguous run of layer l-1 nodes sharing code >> 3 (at
 // most 8). Each thread first loads all its children's records together
 // (one memory latency instead of one per child), then sums them in child

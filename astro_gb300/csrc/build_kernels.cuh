@@ -116,6 +116,8 @@ struct TraverseArgs {
     uint32_t frontier_cap;
     uint32_t nsys;
     float far2;               // group walk: far_ratio^2 (0: no far nodes)
+    uint32_t group_chunk;     // group walk: groups visited in scrambled chunks of this
+                              // many (0: in queue order)
 };
 
 cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,

@@ -339,6 +339,10 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     a.queue = ctx->counters + 1;
     a.delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
     a.far2 = ctx->p.far_ratio * ctx->p.far_ratio;
+    // Groups are queued system by system; for a batch, visiting them in
+    // scrambled chunks of 256 measured 4% faster (a single system: 0-2%
+    // slower, so it keeps the Morton order).
+    a.group_chunk = ctx->nsys > 1 ? 256u : 0u;
     a.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.node_crit2 = ctx->node_crit2;
     a.node_q = ctx->node_q;

@@ -621,6 +621,14 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
         if (lane == 0) gi = atomicAdd(a.queue, 1u);
         gi = __shfl_sync(kFullMask, gi, 0);
         if (gi >= ngroups) break;
+        if (a.group_chunk > 0) {
+            // Queue tickets visit whole chunks of consecutive groups in a
+            // scrambled chunk order (a bijection: 1000003 is prime and
+            // larger than the chunk count); the partial last chunk stays.
+            const uint32_t chunk = a.group_chunk, nfull = ngroups / chunk;
+            if (gi < nfull * chunk)
+                gi = (uint32_t)(((uint64_t)(gi / chunk) * 1000003ull) % nfull) * chunk + gi % chunk;
+        }
         const uint2 gr = a.groups[gi];
         const uint32_t gcount = gr.y - gr.x;
         // A group of at most 16 particles runs as reps = 32 / gcount copies

@@ -158,6 +158,37 @@ class Simulation:
         """Run `steps` full steps (graph-replayed unless FLAG_NO_GRAPH)."""
         self._check(lib().astro_step(self._h, dt, steps))
 
+    def draw_batched(self, dt: float, steps: int, sizes) -> None:
+        """`steps` steps of the systems uploaded by upload_systems (sizes must
+        equal them)."""
+        sz = np.ascontiguousarray(sizes, dtype=np.uint32)
+        self._check(lib().astro_step_batched(self._h, ptr(sz), len(sz), dt, steps))
+
+    def autotune(self, path=None, target: float = 1e-3, samples: int = 1024) -> dict:
+        """Native autotuner (astro_autotune_ex) on the current particles: the
+        best knobs are applied to this context; returns the result record
+        (knobs, step time, error, trials)."""
+        import json
+        import os
+        import tempfile
+
+        tmp = None
+        if path is None:
+            fd, tmp = tempfile.mkstemp(suffix=".json")
+            os.close(fd)
+            path = tmp
+        try:
+            self._check(lib().astro_autotune_ex(self._h, str(path).encode(), target, samples))
+            with open(path) as f:
+                out = json.load(f)
+        finally:
+            if tmp:
+                os.unlink(tmp)
+        p = L.Params()
+        self._check(lib().astro_get_params(self._h, byref(p)))
+        self.params = p
+        return out
+
     def synchronize(self) -> None:
         self._check(lib().astro_synchronize(self._h))
 

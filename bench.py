@@ -94,6 +94,23 @@ def parse():
     return ap.parse_args()
 
 
+CLIMB_MIN_NODES = 32768  # build.cu: layers of at least this capacity get a launch each
+
+
+def kernels_per_step(key_bits: int, layer_sizes) -> int:
+    """This library's kernel launches in one step. PHYSICAL: bbox, setup,
+    encode, sort histogram + one pass per 8 key bits, Morton reorder,
+    topology, the per-layer aggregations below the climb + the climbing
+    one, traversal. REFERENCE: encode, sort histogram + passes, topology,
+    aggregations, traversal, lights snapshot + lighting, integrate. Both
+    come to 8 + passes + the per-layer aggregation launches."""
+    passes = (key_bits + 7) // 8
+    l0 = 0
+    while l0 + 1 < len(layer_sizes) and layer_sizes[l0] >= CLIMB_MIN_NODES:
+        l0 += 1
+    return 8 + passes + l0
+
+
 def walk_flags(args, L, flags):
     """Traversal flags: the preset's defaults adjusted by --walk/--monopole."""
     if args.walk == "particle":
@@ -509,8 +526,7 @@ def run_ours(args, world, rank, local):
         for s1 in sims:
             s1.close()
 
-    passes = (key_bits + 7) // 8
-    launches_per_step = 7 + passes + (p.lbits + 1)
+    launches_per_step = kernels_per_step(key_bits, sizes_)
     sim.close()
     return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
                 wall=wall,

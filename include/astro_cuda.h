@@ -246,6 +246,11 @@ int astro_integrate(astro_ctx* ctx, float dt); /* updateSpheres (BarnesHut.metal
  * a CUDA graph once per upload/params/dt and replayed (ASTRO_FLAG_NO_GRAPH
  * launches it directly). */
 int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps);
+/* astro_step for a batch of independent systems: sys_sizes must equal the
+ * systems given to astro_upload_systems (ASTRO_ERR_INVALID_ARGUMENT
+ * otherwise); all systems advance together in one step graph. */
+int astro_step_batched(astro_ctx* ctx, const uint32_t* sys_sizes, uint32_t nsys, float dt,
+                       uint32_t nsteps);
 int astro_synchronize(astro_ctx* ctx);
 
 /* Readbacks (wait for the stream). */
@@ -362,6 +367,18 @@ int astro_load_state(const char* path, uint32_t max_n, astro_ctx** out, uint64_t
 
 /* Device pointer access for callers that own their own kernels. */
 int astro_get_stream(astro_ctx* ctx, void** stream);
+
+/* Autotune the knobs of a PHYSICAL context on its current particles: the
+ * launch knobs (lbits, bucket, group_size, block_warps, sort_variant), kept
+ * within a median relative acceleration error of max(target, 1.02 x the
+ * starting error) against the FP64 direct sum on sampled particles, and
+ * the accuracy knobs (open_delta_weight, far_ratio) within max(0.8 x
+ * target, 1.02 x the starting error). Steps are timed with dt = 0, so the
+ * particles are unchanged. The best setting is applied to the context and,
+ * when path is not NULL, written there as JSON (knobs, step time, error,
+ * every trial). astro_autotune: target 1e-3, 1,024 samples. */
+int astro_autotune(astro_ctx* ctx, const char* path);
+int astro_autotune_ex(astro_ctx* ctx, const char* path, float target, uint32_t samples);
 
 const char* astro_last_error(const astro_ctx* ctx);
 const char* astro_version(void);

@@ -90,3 +90,17 @@ def test_bench_reference_arm_prints_the_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert line["config"]["workload"].startswith("c1") and line["config"]["n"] == 16384
+
+
+def test_bench_kernel_count_per_step():
+    # The launch list of one c2 step before the climbing build: 3 (bbox,
+    # setup, encode) + histogram + 5 passes + reorder + topology + 13
+    # aggregations + traversal = 25; the climb folds the layers under 32,768
+    # nodes into one launch.
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    c2_layers = [524288] * 6 + [262144, 32768, 4096, 512, 64, 8, 1]
+    assert bench.kernels_per_step(36, c2_layers) == 8 + 5 + 8
+    assert bench.kernels_per_step(18, [205] * 7) == 8 + 3
+    assert bench.kernels_per_step(21, [2 ** 21, 2 ** 18, 2 ** 15, 4096, 512, 64, 8, 1]) == 8 + 3 + 3
