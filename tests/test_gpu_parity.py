@@ -550,15 +550,16 @@ def _degenerate(case):
 
 
 @pytest.mark.parametrize("case", ["one", "two", "coincident", "line", "sheet"])
-@pytest.mark.parametrize("form", [0, 1])
-def test_degenerate_inputs_bit_exact(ag, oracle, case, form):
+@pytest.mark.parametrize("form,far", [(0, 0.0), (1, 0.0), (0, 0.5), (1, 0.3)])
+def test_degenerate_inputs_bit_exact(ag, oracle, case, form, far):
     """Boxes of zero extent in some or all axes, a single particle, and many
-    coincident particles (one leaf): same tree, forces and state as the CPU
-    restatement, and finite everywhere."""
+    coincident particles (one leaf), with and without far nodes (group
+    boxes and displacements of zero length): same tree, forces and state as
+    the CPU restatement, and finite everywhere."""
     L = ag.layouts
     pos = _degenerate(case)
     pm, vr = particles(L, pos, masses=np.full(len(pos), 1.0 / len(pos)))
-    p = ag.default_params(L.PRESET_PHYSICAL, lbits=10, form=form, softening=0.01,
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=10, form=form, softening=0.01, far_ratio=far,
                           flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
     out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2)
     pm_o, vr_o = pm.copy(), vr.copy()
