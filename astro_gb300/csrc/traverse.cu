@@ -285,6 +285,57 @@ __device__ __forceinline__ void far_coefs(float4 cm, float4 q, float qyz, float 
         f.ka = 0.f;
         f.nu = 15.0f * m * R7;
     }
+    if constexpr (!kExact) {
+        // Fast form: the same coefficients from shared products, each FMA
+        // chain ending in its sum. With P = D D^T, u = ga q, M = ga Q and
+        // t = nu/3 D + ka q:
+        //   J_ij  = u_i D_j + u_j D_i - be P_ij - R^5 Q_ij (+ al if i = j)
+        //   H_ijk = t_i P_jk + t_j P_ik + t_k P_ij + M_ij D_k + M_ik D_j + M_jk D_i
+        //           + (u_k - be D_k) [i=j] + (u_j - be D_j) [i=k] + (u_i - be D_i) [j=k]
+        const float* D = f.D;
+        const float P[3][3] = {{D[0] * D[0], D[0] * D[1], D[0] * D[2]},
+                               {D[0] * D[1], D[1] * D[1], D[1] * D[2]},
+                               {D[0] * D[2], D[1] * D[2], D[2] * D[2]}};
+        const float nbe = -f.be, nR5 = -R5, nu3 = f.nu * (1.0f / 3.0f);
+        float u[3], t[3], v[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            u[i] = f.ga * f.qv[i];
+            t[i] = fmaf(nu3, D[i], f.ka * f.qv[i]);
+            v[i] = fmaf(nbe, D[i], u[i]);  // u_i - be D_i
+            fc[i] = fmaf(f.al, D[i], fmaf(nR5, f.qv[i], fc[i]));
+        }
+        float M[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) M[i][j] = f.ga * f.Q[i][j];
+        auto jc = [&](int i, int j, float acc) {
+            acc = fmaf(nR5, f.Q[i][j], fmaf(nbe, P[i][j], acc));
+            return fmaf(u[i], D[j], fmaf(u[j], D[i], acc));
+        };
+        fc[3] = jc(0, 0, fc[3] + f.al);
+        fc[4] = jc(1, 1, fc[4] + f.al);
+        fc[5] = jc(2, 2, fc[5] + f.al);
+        fc[6] = jc(0, 1, fc[6]);
+        fc[7] = jc(0, 2, fc[7]);
+        fc[8] = jc(1, 2, fc[8]);
+        auto hc = [&](int i, int j, int k, float acc) {
+            acc = fmaf(t[i], P[j][k], fmaf(t[j], P[i][k], fmaf(t[k], P[i][j], acc)));
+            return fmaf(M[i][j], D[k], fmaf(M[i][k], D[j], fmaf(M[j][k], D[i], acc)));
+        };
+        fc[9] = hc(0, 0, 0, fmaf(3.0f, v[0], fc[9]));
+        fc[10] = hc(1, 1, 1, fmaf(3.0f, v[1], fc[10]));
+        fc[11] = hc(2, 2, 2, fmaf(3.0f, v[2], fc[11]));
+        fc[12] = hc(0, 0, 1, fc[12] + v[1]);
+        fc[13] = hc(0, 0, 2, fc[13] + v[2]);
+        fc[14] = hc(0, 1, 1, fc[14] + v[0]);
+        fc[15] = hc(1, 1, 2, fc[15] + v[2]);
+        fc[16] = hc(0, 2, 2, fc[16] + v[0]);
+        fc[17] = hc(1, 2, 2, fc[17] + v[1]);
+        fc[18] = hc(0, 1, 2, fc[18]);
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
         fc[i] = xadd<kExact>(fc[i], xfma<kExact>(f.al, f.D[i], -xmul<kExact>(R5, f.qv[i])));
