@@ -46,6 +46,9 @@ public:
         : ctx_(ctx), target_(target), n_samples_(n_samples) {}
 
     int run(const char* path);
+    // The context's parameters before tuning, with its particles uploaded
+    // again if a trial changed the tree depth.
+    int restore(const astro_params& before);
 
 private:
     astro_ctx* ctx_;
@@ -81,6 +84,15 @@ private:
     int sweep(Knob knob, double limit, Trial* best);
     int write(const char* path, const Trial& best, double bound, double acc_bound) const;
 };
+
+int Tuner::restore(const astro_params& before) {
+    int r = astro_set_params(ctx_, &before);
+    if (r != ASTRO_OK || ctx_->uploaded || pm_.empty()) return r;
+    return sizes_.size() > 1
+               ? astro_upload_systems(ctx_, pm_.data(), vr_.data(), sizes_.data(), (uint32_t)sizes_.size())
+               : astro_upload(ctx_, pm_.data(), vr_.data(), nullptr, (uint32_t)pm_.size(),
+                              (uint32_t)pm_.size());
+}
 
 // Applies a setting; a new tree depth needs the particles uploaded again.
 int Tuner::apply(const Knobs& k) {
@@ -302,7 +314,11 @@ extern "C" int astro_autotune_ex(astro_ctx* ctx, const char* path, float target,
     Tuner t(ctx, target, samples);
     const astro_params before = ctx->p;
     const int r = t.run(path);
-    if (r != ASTRO_OK && ctx->p.lbits == before.lbits) astro_set_params(ctx, &before);
+    if (r != ASTRO_OK) {
+        const std::string why = ctx->last_error;
+        t.restore(before);
+        ctx->last_error = why;
+    }
     return r;
 }
 

@@ -54,7 +54,7 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one traversal
 # launch, captured with ncu on GB300 for (workload, form, walk) at the tuned
 # knobs: the roofline's "traffic".
-NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 49.2e6}
+NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 48.9e6}
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -266,8 +266,9 @@ def stage_bytes(n, key_bits, layer_counts, nsys, precision):
     (key and index read and written; 4 B less on the first pass, whose
     indices are generated), then the reorder reads the permutation and
     moves position, velocity and id (and the FP64 position).
-    build: keys read once by the topology pass, which writes two 4-byte
-    links per node; positions read once by the leaf pass; every node written
+    build: keys read once by the topology pass, which writes three 4-byte
+    links per node (first particle, first child, parent); positions read
+    once by the leaf pass; every node written
     once (key 8, sums 16/32, centre of mass 16, ranges 16, quadrupole 20,
     opening radius 4) and read once by its parent (sums, centre of mass,
     quadrupole, range: 68/84).
@@ -283,7 +284,7 @@ def stage_bytes(n, key_bits, layer_counts, nsys, precision):
     return {
         "bbox+encode": (2 * (x64 or 16) + 8) * n,
         "sort+reorder": (8 + 24 * passes - 4) * n + (4 + 2 * (16 + 16 + 4 + x64)) * n,
-        "build": (8 + 16 + x64) * n + nodes * (8 + s_node) + children * child_read,
+        "build": (8 + 16 + x64) * n + nodes * (12 + s_node) + children * child_read,
         "integrate": (80 + 2 * x64) * n,
     }
 

@@ -376,7 +376,8 @@ int astro_get_stream(astro_ctx* ctx, void** stream);
  * target, 1.02 x the starting error). Steps are timed with dt = 0, so the
  * particles are unchanged. The best setting is applied to the context and,
  * when path is not NULL, written there as JSON (knobs, step time, error,
- * every trial). astro_autotune: target 1e-3, 1,024 samples. */
+ * every trial); on failure the context keeps its parameters and particles.
+ * astro_autotune: target 1e-3, 1,024 samples. */
 int astro_autotune(astro_ctx* ctx, const char* path);
 int astro_autotune_ex(astro_ctx* ctx, const char* path, float target, uint32_t samples);
 

@@ -1,5 +1,6 @@
 """The library's native autotuner (astro_autotune_ex) and the batched step
 entry (astro_step_batched), through the C ABI."""
+import ctypes
 import json
 
 import numpy as np
@@ -94,3 +95,25 @@ def test_step_batched_equals_step(ag):
                 sim.draw(1e-3, 3)
             outs.append(sim.download())
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_autotune_failure_keeps_the_context(ag, tmp_path):
+    # An unwritable result path fails the call after the search; the
+    # context keeps its parameters and particles and still steps.
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    pm, vr = ic.plummer(4096, seed=11)
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=8, softening=0.01)
+    with ag.Simulation(p, max_n=len(pm)) as sim:
+        sim.upload(pm, vr)
+        pm0, vr0 = sim.download()
+        with pytest.raises(ag.AstroError):
+            sim.autotune(path=tmp_path / "missing_dir" / "tune.json", samples=64)
+        q = ag.Params()
+        assert ag._native.lib().astro_get_params(sim._h, ctypes.byref(q)) == 0
+        assert bytes(q) == bytes(p)
+        pm1, vr1 = sim.download()
+        assert np.array_equal(pm0, pm1) and np.array_equal(vr0, vr1)
+        sim.draw(1e-3, 1)
+        sim.synchronize()
