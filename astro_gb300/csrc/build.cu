@@ -379,9 +379,24 @@ __device__ __forceinline__ float4 com_from_sums(double sx, double sy, double sz,
                        __double2float_rn(__dmul_rn(sz, inv)), __double2float_rn(m));
 }
 
-__device__ __forceinline__ void emit_group(const AggArgs& a, uint32_t b, uint32_t e) {
-    const uint32_t slot = atomicAdd(a.group_count, 1u);
-    a.groups[slot] = make_uint2(b, e);
+// Slots for c groups of this thread: the active lanes of the warp add their
+// counts and one lane claims them with a single atomic (one atomic per warp
+// instead of one per group on the shared counter); lanes take their runs in
+// lane order.
+__device__ __forceinline__ uint32_t reserve_groups(uint32_t* counter, uint32_t c) {
+    const uint32_t mask = __activemask();
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t prefix = 0, total = 0;
+    for (uint32_t m = mask; m != 0u; m &= m - 1u) {
+        const uint32_t l = (uint32_t)__ffs(m) - 1u;
+        const uint32_t cl = __shfl_sync(mask, c, l);
+        if (l < lane) prefix += cl;
+        total += cl;
+    }
+    const uint32_t leader = (uint32_t)__ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane == leader && total != 0u) base = atomicAdd(counter, total);
+    return __shfl_sync(mask, base, leader) + prefix;
 }
 
 // aggregateLeafNodes (Octree.metal:53-117), one thread per leaf.
@@ -461,8 +476,10 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
         if (a.want_delta) a.node_crit2[j] = node_crit2(a, key, 0, cm);
         // A leaf holding more than one group is cut into group-sized chunks.
         const uint32_t gs = a.group_size;
-        if (pe - pb > gs)
-            for (uint32_t b = pb; b < pe; b += gs) emit_group(a, b, min(b + gs, pe));
+        const uint32_t c = pe - pb > gs ? (pe - pb + gs - 1u) / gs : 0u;
+        const uint32_t slot = reserve_groups(a.group_count, c);
+        for (uint32_t i = 0; i < c; ++i)
+            a.groups[slot + i] = make_uint2(pb + i * gs, min(pb + (i + 1u) * gs, pe));
     }
 }
 
@@ -599,38 +616,49 @@ __device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32
         // small children (greedy, in child order); a small top-layer node is
         // a group by itself.
         const uint32_t gs = a.group_size;
-        if (pe - pb > gs) {
-            uint2 cr[8];
+        uint2 cr[8];
+        const bool split = pe - pb > gs;
+        if (split) {
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
                 const uint4 rng = k < nch ? ld_l2(a.node_rng + cb + k) : make_uint4(0u, 0u, 0u, 0u);
                 cr[k] = make_uint2(rng.z, rng.w);
             }
-            uint32_t gb = 0, ge = 0;
-#pragma unroll
-            for (uint32_t k = 0; k < 8; ++k) {
-                if (k >= nch) break;
-                const uint32_t cc = cr[k].y - cr[k].x;
-                if (cc <= gs) {
-                    if (ge == gb) {
-                        gb = cr[k].x;
-                        ge = cr[k].y;
-                    } else if ((ge - gb) + cc <= gs) {
-                        ge = cr[k].y;
-                    } else {
-                        emit_group(a, gb, ge);
-                        gb = cr[k].x;
-                        ge = cr[k].y;
-                    }
-                } else if (ge != gb) {
-                    emit_group(a, gb, ge);
-                    gb = ge = 0;
-                }
-            }
-            if (ge != gb) emit_group(a, gb, ge);
-        } else if (l == a.lbits) {
-            emit_group(a, pb, pe);
         }
+        // The packing runs twice: to count the groups, then to write them
+        // into the slots reserved for this node.
+        auto pack = [&](auto&& emit) {
+            if (split) {
+                uint32_t gb = 0, ge = 0;
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) {
+                    if (k >= nch) break;
+                    const uint32_t cc = cr[k].y - cr[k].x;
+                    if (cc <= gs) {
+                        if (ge == gb) {
+                            gb = cr[k].x;
+                            ge = cr[k].y;
+                        } else if ((ge - gb) + cc <= gs) {
+                            ge = cr[k].y;
+                        } else {
+                            emit(gb, ge);
+                            gb = cr[k].x;
+                            ge = cr[k].y;
+                        }
+                    } else if (ge != gb) {
+                        emit(gb, ge);
+                        gb = ge = 0;
+                    }
+                }
+                if (ge != gb) emit(gb, ge);
+            } else if (l == a.lbits) {
+                emit(pb, pe);
+            }
+        };
+        uint32_t c = 0;
+        pack([&](uint32_t, uint32_t) { ++c; });
+        uint32_t slot = reserve_groups(a.group_count, c);
+        pack([&](uint32_t b, uint32_t e) { a.groups[slot++] = make_uint2(b, e); });
     }
 }
 
