@@ -15,6 +15,8 @@ The knobs are fields of astro_params that change speed, not physics:
                 is summed particle by particle
   sort_variant  radix sort pass kernel (items per thread / blocks per SM /
                 ranking / pipelined)
+  walk_frontier the group walk's frontier: runs of consecutive child nodes
+                or a list of node indices
 
   far_ratio     accepted nodes further than (group radius) / far_ratio from
                 the group's centre are summed through one second-order
@@ -32,8 +34,8 @@ theta, the softening, the quadrupole and opening-radius flags and the form
 
 Search: coordinate descent from the preset's defaults over the speed knobs,
 then every (open_delta_weight, far_ratio) pair (far_ratio rising until the
-error leaves its bound), then lbits, bucket, group_size and block_warps once
-more. Each knob in turn is swept with the others fixed; the fastest setting
+error leaves its bound), then lbits, bucket, group_size, block_warps and
+walk_frontier once more. Each knob in turn is swept with the others fixed; the fastest setting
 is kept among those whose
 median relative acceleration error against the FP64 direct sum (on sampled
 particles) is at most max(target, 1.02 x the starting error) (max(0.8 x the
@@ -62,8 +64,8 @@ from .simulation import Simulation, default_params
 from .workloads import WORKLOADS
 
 TUNED_PATH = Path(__file__).resolve().parent / "tuned.json"
-KNOBS = ("lbits", "bucket", "group_size", "block_warps", "sort_variant", "far_ratio",
-         "open_delta_weight")
+KNOBS = ("lbits", "bucket", "group_size", "block_warps", "sort_variant", "walk_frontier",
+         "far_ratio", "open_delta_weight")
 ACCURACY_KNOBS = ("far_ratio", "open_delta_weight")
 FORMS = {"plain": L.FORM_PLAIN, "precision": L.FORM_PRECISION}
 
@@ -83,6 +85,8 @@ def candidates(knob: str, n: int) -> list[int]:
         return [4, 8]
     if knob == "sort_variant":
         return list(range(1, 10))
+    if knob == "walk_frontier":
+        return [0, 1]
     if knob == "far_ratio":
         return [0.1, 0.15, 0.2, 0.25, 0.3, 0.4, 0.5]
     if knob == "open_delta_weight":

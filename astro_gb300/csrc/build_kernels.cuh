@@ -118,6 +118,7 @@ struct TraverseArgs {
     float far2;               // group walk: far_ratio^2 (0: no far nodes)
     uint32_t group_chunk;     // group walk: groups visited in scrambled chunks of this
                               // many (0: in queue order)
+    uint32_t walk_runs;       // group walk: frontier of runs (1) or of node indices (0)
 };
 
 cudaError_t launch_encode_ref(const float4* pos, uint64_t* codes, uint32_t n_tree, uint32_t lbits,

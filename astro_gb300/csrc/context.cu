@@ -95,6 +95,8 @@ int validate_params(const astro_params* p, const char** why) {
         return (*why = "open_delta_weight must be finite and >= 0", ASTRO_ERR_INVALID_ARGUMENT);
     if (!(p->far_ratio >= 0.0f && p->far_ratio <= 0.5f))
         return (*why = "far_ratio must be in [0, 0.5]", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->walk_frontier > 1)
+        return (*why = "walk_frontier must be 0 (runs) or 1 (node list)", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->light_sources > 0 && p->preset != ASTRO_PRESET_REFERENCE)
         return (*why = "the lighting pass needs the REFERENCE preset", ASTRO_ERR_INVALID_ARGUMENT);
     return ASTRO_OK;
@@ -343,6 +345,7 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     // scrambled chunks of 256 measured 4% faster (a single system: 0-2%
     // slower, so it keeps the Morton order).
     a.group_chunk = ctx->nsys > 1 ? 256u : 0u;
+    a.walk_runs = ctx->p.walk_frontier == 0 ? 1u : 0u;
     a.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
     a.node_crit2 = ctx->node_crit2;
     a.node_q = ctx->node_q;

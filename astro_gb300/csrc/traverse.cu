@@ -615,8 +615,10 @@ __global__ __launch_bounds__(kWarps * 32) void traverse_phys_kernel(TraverseArgs
 // the tree breadth first from the system's root, testing 32 frontier nodes
 // at a time against the group's bounding box: accepted nodes go to the cell
 // list (records staged in shared memory), opened leaves and buckets to the
-// leaf list, other opened nodes put their children in the next frontier
-// (per-warp buffers in global memory). Lists are evaluated by all lanes,
+// leaf list, other opened nodes put their children (one run of consecutive
+// node indices each) in the next frontier (per-warp buffers in global
+// memory); accepted nodes far from the group go to the far list, expanded
+// after the walk. The cell and leaf lists are evaluated by all lanes,
 // one particle per lane, whenever they fill and at the end: cells into one
 // sum, leaf particles (32 at a time through shared memory) into another.
 // Cell list capacity per warp: the largest that keeps a block's static
@@ -644,6 +646,8 @@ struct CellSlot<false> {
 #ifndef ASTRO_GROUP_WARPS_PER_SM
 #define ASTRO_GROUP_WARPS_PER_SM 24
 #endif
+
+
 #if ASTRO_GROUP_WARPS_PER_SM > 0
 #define ASTRO_GROUP_BOUNDS(w) __launch_bounds__((w) * 32, ASTRO_GROUP_WARPS_PER_SM / (w))
 #else
@@ -892,6 +896,131 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             n_leaf = 0;
         };
 
+        // Two forms of the same breadth-first walk (same nodes, same order):
+        // a frontier of runs of consecutive child nodes, or of node indices;
+        // which is faster depends on the workload (astro_params.walk_frontier).
+        if (a.walk_runs) {
+        // The frontier holds runs of consecutive node indices (first, count)
+        // in walk order: the children of an opened node are consecutive, so
+        // each opened node adds one run, and a chunk of 32 nodes is found by
+        // a shuffle search over 32 runs loaded at once, without a load of
+        // its own.
+        uint2* cur = reinterpret_cast<uint2*>(buf0);
+        uint2* nxt = reinterpret_cast<uint2*>(buf1);
+        const uint32_t run_cap = a.frontier_cap / 2u;
+        if (lane == 0) cur[0] = make_uint2(a.sys[sys].root, 1u);
+        uint32_t ncur = 1;
+        int layer = (int)a.lbits;
+        __syncwarp();
+        while (ncur > 0) {
+            uint32_t nnext = 0;
+            for (uint32_t rb = 0; rb < ncur; rb += 32u) {
+                const uint32_t nrun = min(32u, ncur - rb);
+                const uint2 run = lane < nrun ? cur[rb + lane] : make_uint2(0u, 0u);
+                uint32_t rincl = run.y;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFullMask, rincl, o);
+                    if (lane >= (uint32_t)o) rincl += y;
+                }
+                const uint32_t rpre = rincl - run.y;
+                const uint32_t rtotal = __shfl_sync(kFullMask, rincl, 31);
+                for (uint32_t t0 = 0; t0 < rtotal; t0 += 32u) {
+                    const uint32_t pos = t0 + lane;
+                    const bool has = pos < rtotal;
+                    // The run holding position pos: the last one starting at or before it.
+                    uint32_t e = 0;
+#pragma unroll
+                    for (uint32_t step = 16; step > 0; step >>= 1) {
+                        const uint32_t cand = e + step;
+                        const uint32_t pc = __shfl_sync(kFullMask, rpre, cand & 31u);
+                        if (cand < nrun && pc <= pos) e = cand;
+                    }
+                    const uint32_t first = __shfl_sync(kFullMask, run.x, e);
+                    const uint32_t estart = __shfl_sync(kFullMask, rpre, e);
+                    const uint32_t nd = has ? first + (pos - estart) : 0u;
+                    float4 c = make_float4(0.f, 0.f, 0.f, 0.f), q4 = c;
+                    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+                    float crit = 0.f, qyz = 0.f;
+                    if (has) {
+                        c = __ldg(&a.node_cm[nd]);
+                        r = __ldg(&a.node_rng[nd]);
+                        crit = a.delta ? __ldg(&a.node_crit2[nd]) : __ldg(&crit_layer[layer]);
+                    }
+                    const float bx = fmaxf(fmaxf(__fsub_rn(lo_x, c.x), __fsub_rn(c.x, hi_x)), 0.f);
+                    const float by = fmaxf(fmaxf(__fsub_rn(lo_y, c.y), __fsub_rn(c.y, hi_y)), 0.f);
+                    const float bz = fmaxf(fmaxf(__fsub_rn(lo_z, c.z), __fsub_rn(c.z, hi_z)), 0.f);
+                    const float dist2 =
+                        __fadd_rn(__fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
+                    const bool accepted = has && dist2 > crit;
+                    const bool leaf = has && !accepted && (layer == 0 || r.w - r.z <= a.bucket);
+                    const bool opn = has && !accepted && !leaf;
+                    bool far = false;
+                    if (far_on && accepted) {
+                        const float Dx = __fsub_rn(c.x, gcx), Dy = __fsub_rn(c.y, gcy),
+                                    Dz = __fsub_rn(c.z, gcz);
+                        const float D2 = __fadd_rn(__fmul_rn(Dx, Dx),
+                                                   __fadd_rn(__fmul_rn(Dy, Dy), __fmul_rn(Dz, Dz)));
+                        far = __fmul_rn(a.far2, D2) > rg2;
+                    }
+                    const bool acc = accepted && !far;
+                    const uint32_t tested = __popc(__ballot_sync(kFullMask, has));
+                    if (owner) visits += tested;
+                    // Far nodes, in frontier order.
+                    const uint32_t bfar = __ballot_sync(kFullMask, far);
+                    if (bfar) {
+                        if (far_total + __popc(bfar) <= a.frontier_cap) {
+                            if (far) far_list[far_total + __popc(bfar & lt)] = nd;
+                            far_total += __popc(bfar);
+                        } else if (lane == 0) {
+                            atomicOr(a.err, kErrFrontier);
+                        }
+                    }
+                    // Accepted cells, in frontier order.
+                    const uint32_t bacc = __ballot_sync(kFullMask, acc);
+                    if (bacc) {
+                        if (n_cell + __popc(bacc) > (uint32_t)kCellCap) flush_cells();
+                        if (acc) {
+                            const uint32_t slot = n_cell + __popc(bacc & lt);
+                            s_cell[warp][slot].cm = c;
+                            if constexpr (kQuad) {
+                                q4 = __ldg(&a.node_q[nd]);
+                                qyz = __ldg(&a.node_qyz[nd]);
+                                s_cell[warp][slot].q = q4;
+                                s_cell[warp][slot].q2 = make_float4(qyz, -(q4.x + q4.y), 0.f, 0.f);
+                            }
+                        }
+                        n_cell += __popc(bacc);
+                    }
+                    // Opened leaves and buckets, in frontier order.
+                    const uint32_t bleaf = __ballot_sync(kFullMask, leaf);
+                    if (bleaf) {
+                        if (n_leaf + __popc(bleaf) > (uint32_t)kLeafCap) flush_leaves();
+                        if (leaf) s_leaf[warp][n_leaf + __popc(bleaf & lt)] = make_uint2(r.z, r.w);
+                        n_leaf += __popc(bleaf);
+                    }
+                    // Children of opened nodes: one run each, in frontier order.
+                    const uint32_t bopen = __ballot_sync(kFullMask, opn);
+                    if (bopen) {
+                        if (nnext + __popc(bopen) <= run_cap) {
+                            if (opn) nxt[nnext + __popc(bopen & lt)] = make_uint2(r.x, r.y - r.x);
+                            nnext += __popc(bopen);
+                        } else if (lane == 0) {
+                            atomicOr(a.err, kErrFrontier);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            uint2* t = cur;
+            cur = nxt;
+            nxt = t;
+            ncur = nnext;
+            --layer;
+        }
+        } else {
+        // The frontier holds node indices, each opened node adding its
+        // children one by one.
         uint32_t* cur = buf0;
         uint32_t* nxt = buf1;
         if (lane == 0) cur[0] = a.sys[sys].root;
@@ -986,6 +1115,7 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
             nxt = t;
             ncur = nnext;
             --layer;
+        }
         }
         flush_cells();
         flush_leaves();

@@ -5,12 +5,13 @@
 // move, so every trial sees the same input) on the context's own particles
 // and measures each setting's median relative acceleration error against
 // the FP64 direct sum on sampled particles. Search: coordinate descent over
-// the speed knobs (lbits, bucket, group_size, block_warps, sort_variant),
+// the speed knobs (lbits, bucket, group_size, block_warps, sort_variant,
+// walk_frontier),
 // keeping the fastest setting whose error stays within
 // max(target, 1.02 x the starting error); then every (open_delta_weight,
 // far_ratio) pair, far_ratio rising until the error leaves
 // max(0.8 x target, 1.02 x the starting error); then lbits, bucket,
-// group_size and block_warps once more within that bound. sort_variant is
+// group_size, block_warps and walk_frontier once more within that bound. sort_variant is
 // judged by the sort stage's own time. theta, the softening, the walk flags
 // and the form are physics and stay as set.
 #include <algorithm>
@@ -24,12 +25,13 @@
 namespace {
 
 struct Knobs {
-    uint32_t lbits, bucket, group_size, block_warps, sort_variant;
+    uint32_t lbits, bucket, group_size, block_warps, sort_variant, walk_frontier;
     float far_ratio, open_delta_weight;
     bool operator==(const Knobs& o) const {
         return lbits == o.lbits && bucket == o.bucket && group_size == o.group_size &&
                block_warps == o.block_warps && sort_variant == o.sort_variant &&
-               far_ratio == o.far_ratio && open_delta_weight == o.open_delta_weight;
+               walk_frontier == o.walk_frontier && far_ratio == o.far_ratio &&
+               open_delta_weight == o.open_delta_weight;
     }
 };
 
@@ -38,7 +40,7 @@ struct Trial {
     double ms = 0, sort_ms = 0, err = 0;
 };
 
-enum Knob { kLbits, kBucket, kGroupSize, kBlockWarps, kSortVariant };
+enum Knob { kLbits, kBucket, kGroupSize, kBlockWarps, kSortVariant, kWalkFrontier };
 
 class Tuner {
 public:
@@ -65,7 +67,7 @@ private:
 
     Knobs knobs_of(const astro_params& p) const {
         return {p.lbits, p.bucket, p.group_size ? p.group_size : 32u, p.block_warps ? p.block_warps : 4u,
-                p.sort_variant, p.far_ratio, p.open_delta_weight};
+                p.sort_variant, p.walk_frontier, p.far_ratio, p.open_delta_weight};
     }
     astro_params params_of(const Knobs& k) const {
         astro_params p = base_;
@@ -74,6 +76,7 @@ private:
         p.group_size = k.group_size;
         p.block_warps = k.block_warps;
         p.sort_variant = k.sort_variant;
+        p.walk_frontier = k.walk_frontier;
         p.far_ratio = k.far_ratio;
         p.open_delta_weight = k.open_delta_weight;
         return p;
@@ -182,6 +185,7 @@ std::vector<uint32_t> Tuner::candidates(Knob knob) const {
         case kGroupSize: return {8, 12, 16, 24, 32};
         case kBlockWarps: return {4, 8};
         case kSortVariant: return {1, 2, 3, 4, 5, 6, 7, 8, 9};
+        case kWalkFrontier: return {0, 1};
     }
     return {};
 }
@@ -191,7 +195,7 @@ int Tuner::sweep(Knob knob, double limit, Trial* best) {
         Knobs k = best->k;
         uint32_t* field = knob == kLbits ? &k.lbits : knob == kBucket ? &k.bucket
                           : knob == kGroupSize ? &k.group_size : knob == kBlockWarps ? &k.block_warps
-                          : &k.sort_variant;
+                          : knob == kWalkFrontier ? &k.walk_frontier : &k.sort_variant;
         if (*field == v) continue;
         *field = v;
         Trial t;
@@ -207,9 +211,10 @@ void put_knobs(std::string& s, const Knobs& k) {
     char b[256];
     std::snprintf(b, sizeof(b),
                   "{\"lbits\": %u, \"bucket\": %u, \"group_size\": %u, \"block_warps\": %u, "
-                  "\"sort_variant\": %u, \"far_ratio\": %.9g, \"open_delta_weight\": %.9g}",
-                  k.lbits, k.bucket, k.group_size, k.block_warps, k.sort_variant, (double)k.far_ratio,
-                  (double)k.open_delta_weight);
+                  "\"sort_variant\": %u, \"walk_frontier\": %u, \"far_ratio\": %.9g, "
+                  "\"open_delta_weight\": %.9g}",
+                  k.lbits, k.bucket, k.group_size, k.block_warps, k.sort_variant, k.walk_frontier,
+                  (double)k.far_ratio, (double)k.open_delta_weight);
     s += b;
 }
 
@@ -271,7 +276,7 @@ int Tuner::run(const char* path) {
     if ((r = measure(start, &best)) != ASTRO_OK) return r;
     const double bound = std::max((double)target_, 1.02 * best.err);
     const double acc_bound = std::max(0.8 * target_, 1.02 * best.err);
-    for (Knob k : {kLbits, kBucket, kGroupSize, kBlockWarps, kSortVariant})
+    for (Knob k : {kLbits, kBucket, kGroupSize, kBlockWarps, kSortVariant, kWalkFrontier})
         if ((r = sweep(k, bound, &best)) != ASTRO_OK) return r;
     // The accuracy knobs share one error budget.
     const Knobs base = best.k;
@@ -289,7 +294,7 @@ int Tuner::run(const char* path) {
         }
     }
     // The tree and launch knobs again (group boxes also decide far nodes).
-    for (Knob k : {kLbits, kBucket, kGroupSize, kBlockWarps})
+    for (Knob k : {kLbits, kBucket, kGroupSize, kBlockWarps, kWalkFrontier})
         if ((r = sweep(k, acc_bound, &best)) != ASTRO_OK) return r;
     if ((r = apply(best.k)) != ASTRO_OK) return r;
     return path ? write(path, best, bound, acc_bound) : ASTRO_OK;

@@ -77,7 +77,7 @@ class Params(ctypes.Structure):
         ("light_sources", ctypes.c_uint32),
         ("open_delta_weight", ctypes.c_float),
         ("far_ratio", ctypes.c_float),
-        ("_reserved", ctypes.c_uint32 * 1),
+        ("walk_frontier", ctypes.c_uint32),
     ]
 
     def replace(self, **kw) -> "Params":

@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--far-ratio", type=float, default=None,
                     help="group walk: nodes further than (group radius) / r from the group's "
                          "centre are summed through one expansion per group (0: none)")
+    ap.add_argument("--walk-frontier", type=int, default=None, choices=[0, 1],
+                    help="group walk frontier: 0 = runs of consecutive nodes, 1 = node list")
     ap.add_argument("--no-tuned", action="store_true", help="ignore the autotuner's file")
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--persistent", action="store_true")
@@ -130,10 +132,12 @@ def knobs(args):
 
         tuned = autotune.load().get(f"{args.workload}/{args.form}", {}).get("knobs", {})
     default = {"lbits": WORKLOADS[args.workload].lbits, "bucket": 16, "block_warps": 0,
-               "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0, "far_ratio": 0.0}
+               "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0, "far_ratio": 0.0,
+               "walk_frontier": 0}
     given = {"lbits": args.lbits, "bucket": args.bucket, "block_warps": args.warps,
              "group_size": args.group_size, "sort_variant": args.sort_variant,
-             "open_delta_weight": args.delta_weight, "far_ratio": args.far_ratio}
+             "open_delta_weight": args.delta_weight, "far_ratio": args.far_ratio,
+             "walk_frontier": args.walk_frontier}
     out, source = {}, {}
     for k in default:
         if given[k] is not None:
@@ -619,6 +623,7 @@ def config_dict(args, desc, n, dt, p, knob_source):
             "lbits": p.lbits, "bucket": p.bucket, "group_size": p.group_size or 32,
             "block_warps": p.block_warps or 4, "sort_variant": p.sort_variant,
             "open_delta_weight": p.open_delta_weight, "far_ratio": p.far_ratio,
+            "walk_frontier": p.walk_frontier,
             "knob_source": knob_source,
             "l2": "flushed (256 MB write) before every timed step",
             "parallelism": "replicas (one independent system per GPU)"}

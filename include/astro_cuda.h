@@ -197,7 +197,10 @@ typedef struct astro_params {
                                  centre, evaluated at each particle of the
                                  group, instead of term by term; 0 = every
                                  accepted node term by term; 0..0.5 */
-    uint32_t _reserved[1];
+    uint32_t walk_frontier;   /* PHYSICAL group walk, the frontier's form: 0 = runs
+                                 of consecutive child nodes (one per opened
+                                 node), 1 = a list of node indices; same walk,
+                                 same results, different speed per workload */
 } astro_params;
 
 /* Fill *out with the defaults of a preset. */

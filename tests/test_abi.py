@@ -59,6 +59,7 @@ _Static_assert(offsetof(astro_params, group_size) == 64, "group_size");
 _Static_assert(offsetof(astro_params, sort_variant) == 68, "sort_variant");
 _Static_assert(offsetof(astro_params, open_delta_weight) == 76, "open_delta_weight");
 _Static_assert(offsetof(astro_params, far_ratio) == 80, "far_ratio");
+_Static_assert(offsetof(astro_params, walk_frontier) == 84, "walk_frontier");
 _Static_assert(sizeof(astro_params) == 88, "astro_params");
 _Static_assert(sizeof(astro_state_header) == 136, "astro_state_header");
 _Static_assert(offsetof(astro_state_header, params) == 16, "state params");
@@ -133,6 +134,8 @@ def test_argument_errors_without_device(native):
     bad = p.replace(sort_variant=10)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(open_delta_weight=-1.0)
+    assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
+    bad = p.replace(walk_frontier=2)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     for ratio in (-0.1, 0.6, float("nan")):
         bad = p.replace(far_ratio=ratio)

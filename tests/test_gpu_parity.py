@@ -688,3 +688,38 @@ def test_build_per_layer_and_climbing_bit_exact(ag, oracle, form):
     assert_tree_equal(out, ref)
     assert np.array_equal(out["acc4"], ref["acc4"])
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
+
+
+@pytest.mark.parametrize("case", ["plain", "far", "precision-far", "batched", "small-groups"])
+def test_node_list_frontier_bit_exact(ag, oracle, case):
+    """The group walk's other frontier form (a list of node indices instead
+    of runs) visits the same nodes in the same order: every result equals
+    the restatement's."""
+    from astro_gb300 import ic
+
+    L = ag.layouts
+    kw = dict(lbits=10, walk_frontier=1, flags=WALKS["group"](L) | L.FLAG_IEEE_EXACT)
+    sizes = None
+    if case == "far":
+        kw.update(far_ratio=0.3)
+    elif case == "precision-far":
+        kw.update(far_ratio=0.2, form=L.FORM_PRECISION)
+    elif case == "small-groups":
+        kw.update(group_size=5)
+    if case == "batched":
+        sizes = [1, 2, 31, 33, 1024, 5000, 64, 3, 4096, 777]
+        parts = [ic.plummer(s_, seed=1004, a=0.5 + 0.1 * k, system=k) for k, s_ in enumerate(sizes)]
+        pm = np.concatenate([a_ for a_, _ in parts])
+        vr = np.concatenate([b_ for _, b_ in parts])
+        kw.update(far_ratio=0.25)
+    else:
+        pm, vr = ic.plummer(16384, seed=1001)
+    p = ag.default_params(L.PRESET_PHYSICAL, **kw)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=2, sizes=sizes)
+    pm_o, vr_o = pm.copy(), vr.copy()
+    ref = oracle.phys_run(p, pm_o, vr_o, sizes=sizes, dt=1e-3, steps=2)
+    assert_tree_equal(out, ref)
+    for k in ("interactions", "node_visits", "far_nodes", "far_interactions"):
+        assert out[k] == ref[k], k
+    assert np.array_equal(out["acc4"], ref["acc4"])
+    assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)

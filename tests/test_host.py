@@ -48,10 +48,10 @@ def test_tuned_file_feeds_bench_knobs(tmp_path, monkeypatch):
 
     args = SimpleNamespace(workload="c2", form="plain", no_tuned=False, lbits=None, bucket=20,
                            warps=None, group_size=None, sort_variant=None, delta_weight=None,
-                           far_ratio=None)
+                           far_ratio=None, walk_frontier=None)
     k, src = bench.knobs(args)
     assert k == {"lbits": 12, "bucket": 20, "block_warps": 8, "group_size": 16, "sort_variant": 3,
-                 "open_delta_weight": 1.0, "far_ratio": 0.0}
+                 "open_delta_weight": 1.0, "far_ratio": 0.0, "walk_frontier": 0}
     assert src["bucket"] == "command line" and src["lbits"] == "autotuner"
     args.form = "precision"  # no entry: preset defaults
     k, src = bench.knobs(args)
