@@ -54,7 +54,7 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one traversal
 # launch, captured with ncu on GB300 for (workload, form, walk) at the tuned
 # knobs: the roofline's "traffic".
-NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 48.9e6}
+NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 51.2e6}
 
 def parse():
     ap = argparse.ArgumentParser()
