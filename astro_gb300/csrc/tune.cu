@@ -46,6 +46,12 @@ class Tuner {
 public:
     Tuner(astro_ctx* ctx, float target, uint32_t n_samples)
         : ctx_(ctx), target_(target), n_samples_(n_samples) {}
+    ~Tuner() {
+        for (cudaEvent_t& e : ev_)
+            if (e) cudaEventDestroy(e);
+    }
+    Tuner(const Tuner&) = delete;
+    Tuner& operator=(const Tuner&) = delete;
 
     int run(const char* path);
     // The context's parameters before tuning, with its particles uploaded
@@ -263,8 +269,10 @@ int Tuner::run(const char* path) {
     for (uint32_t s = 0; s < ns; ++s) samples_[s] = (uint32_t)(((uint64_t)s * n + n / (2 * ns)) / ns);
     direct_.assign(3ull * ns, 0.0);
     if ((r = astro_direct_accel_f64(ctx_, samples_.data(), ns, direct_.data())) != ASTRO_OK) return r;
-    if (cudaEventCreate(&ev_[0]) != cudaSuccess || cudaEventCreate(&ev_[1]) != cudaSuccess)
+    if (cudaEventCreate(&ev_[0]) != cudaSuccess || cudaEventCreate(&ev_[1]) != cudaSuccess) {
+        ctx_->last_error = "autotune: cudaEventCreate failed";
         return ASTRO_ERR_CUDA;
+    }
 
     Trial best;
     const Knobs start = knobs_of(base_);
