@@ -111,3 +111,32 @@ def test_random_reference_scene_bit_exact(ag, oracle, k):
     assert_tree_equal(out, ref)
     assert np.array_equal(out["acc4"], ref["acc4"]), cfg
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o), cfg
+
+
+@pytest.mark.parametrize("k", range(16))
+def test_random_configuration_fast_within_tolerance(ag, oracle, k):
+    """The fast form (rsqrt, FMAs, replicated small groups, factored far-node
+    coefficients) over random configurations: the same walk (identical
+    counts) and accelerations within the fast path's tolerance."""
+    from astro_gb300 import ic
+    from test_gpu_parity import acc_close, assert_tree_equal, run_gpu
+
+    L = ag.layouts
+    cfg = _config(100 + k)
+    cfg["n"] = max(cfg["n"], 500)
+    flags = (L.FLAG_QUADRUPOLE if cfg["quad"] else 0) | (L.FLAG_OPEN_DELTA if cfg["delta"] else 0)
+    pm, vr, sizes = _particles(L, ic, cfg)
+    nsys = len(sizes) if sizes else 1
+    if 3 * cfg["lbits"] + ((nsys - 1).bit_length() if nsys > 1 else 0) > 64:
+        cfg["lbits"] = 20
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=cfg["lbits"], group_size=cfg["group_size"],
+                          bucket=cfg["bucket"], far_ratio=cfg["far_ratio"],
+                          walk_frontier=cfg["walk_frontier"], form=cfg["form"], softening=0.01,
+                          block_warps=8 if k % 2 else 4, flags=flags)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=1, sizes=sizes)
+    ref = oracle.phys_run(p, pm.copy(), vr.copy(), sizes=sizes, dt=1e-3, steps=1)
+    assert_tree_equal(out, ref)
+    for key in ("interactions", "node_visits", "far_nodes", "far_interactions"):
+        assert out[key] == ref[key], (cfg, key)
+    ok, rel = acc_close(out["acc4"], ref["acc4"])
+    assert ok.all(), f"{cfg}: {(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
