@@ -899,6 +899,9 @@ __global__ ASTRO_GROUP_BOUNDS(kWarps) void traverse_group_kernel(TraverseArgs a)
         // Two forms of the same breadth-first walk (same nodes, same order):
         // a frontier of runs of consecutive child nodes, or of node indices;
         // which is faster depends on the workload (astro_params.walk_frontier).
+        // The per-node test and staging are written out in both forms: shared
+        // through one lambda they compiled to a register allocation with more
+        // spills and a traversal up to 2.4% slower.
         if (a.walk_runs) {
         // The frontier holds runs of consecutive node indices (first, count)
         // in walk order: the children of an opened node are consecutive, so
