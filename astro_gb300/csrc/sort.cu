@@ -224,14 +224,11 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     st_relaxed_u32(my_word, (tile == 0 ? kLbInclusive : kLbAggregate) | tile_cnt);
     const uint32_t tile_start = block_exclusive_scan(tile_cnt, sm.scan_tmp);
     sm.tile_start[tid] = tile_start;
-    uint32_t prefix = 0;
-    if (tile > 0) {
-        prefix = lookback_window(lookback, tile, tid, err);
-        st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
-    }
-    sm.global_base[tid] = excl[tid] + prefix;
     __syncthreads();
 
+    // The tile is staged in sorted order before the look-back: staging needs
+    // only tile-local offsets, and the time it takes is slack in which the
+    // earlier tiles publish their counts.
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const uint32_t digit = (uint32_t)(key[k] >> shift) & dmask;
@@ -246,6 +243,12 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
             sm.u.stage.vals[pos[k]] = val[k];
         }
     }
+    uint32_t prefix = 0;
+    if (tile > 0) {
+        prefix = lookback_window(lookback, tile, tid, err);
+        st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
+    }
+    sm.global_base[tid] = excl[tid] + prefix;
     __syncthreads();
     const uint32_t tile_n = (uint32_t)min((uint64_t)kTile, (uint64_t)n - tile_base);
     for (uint32_t i = tid; i < tile_n; i += kThreads) {
