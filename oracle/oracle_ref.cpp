@@ -22,7 +22,7 @@ constexpr uint32_t kInvalidChild = ASTRO_INVALID_CHILD;       // Octree.metal:10
 constexpr uint32_t kScanBlock = 512;                          // RadixSort.metal:5
 
 // MSL leaves an out-of-range float->uint conversion implementation-defined
-// (MortonCode.metal:35-37). This build defines it as a saturating
+// (MortonCode.metal:35-37). Here it is defined as a saturating
 // round-toward-zero conversion: NaN and values <= 0 give 0, values >= 2^32
 // give 0xFFFFFFFF. The CUDA kernels use the same conversion.
 inline uint32_t float_to_uint_sat(float f) {
