@@ -140,3 +140,40 @@ def test_random_configuration_fast_within_tolerance(ag, oracle, k):
         assert out[key] == ref[key], (cfg, key)
     ok, rel = acc_close(out["acc4"], ref["acc4"])
     assert ok.all(), f"{cfg}: {(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
+
+
+# Full groups (more than 16 particles, so no replication) in the precision
+# form's fast path, which evaluates cells and leaf particles two at a time in
+# packed FP32 pairs; the list lengths of a flush are odd and even alike.
+PAIR_CASES = [
+    dict(n=4097, group_size=32, far_ratio=0.0, walk_frontier=0, nsys=1, dist="plummer"),
+    dict(n=20000, group_size=24, far_ratio=0.3, walk_frontier=1, nsys=1, dist="disk"),
+    dict(n=6001, group_size=32, far_ratio=0.15, walk_frontier=0, nsys=3, dist="cube"),
+    dict(n=12345, group_size=17, far_ratio=0.0, walk_frontier=1, nsys=1, dist="cube"),
+]
+
+
+@pytest.mark.parametrize("k", range(len(PAIR_CASES)))
+def test_precision_pairs_within_tolerance(ag, oracle, k):
+    """Precision form, fast path, quadrupoles and the δ opening: the same
+    tree and counts as the CPU restatement, accelerations within the fast
+    path's tolerance."""
+    from astro_gb300 import ic
+    from test_gpu_parity import acc_close, assert_tree_equal, run_gpu
+
+    L = ag.layouts
+    cfg = dict(lbits=10, bucket=8, quad=True, delta=True, form=L.FORM_PRECISION)
+    cfg.update(PAIR_CASES[k])
+    flags = L.FLAG_QUADRUPOLE | L.FLAG_OPEN_DELTA
+    pm, vr, sizes = _particles(L, ic, cfg)
+    p = ag.default_params(L.PRESET_PHYSICAL, lbits=cfg["lbits"], group_size=cfg["group_size"],
+                          bucket=cfg["bucket"], far_ratio=cfg["far_ratio"],
+                          walk_frontier=cfg["walk_frontier"], form=cfg["form"], softening=0.01,
+                          block_warps=8 if k % 2 else 4, flags=flags)
+    out = run_gpu(ag, p, pm, vr, dt=1e-3, steps=1, sizes=sizes)
+    ref = oracle.phys_run(p, pm.copy(), vr.copy(), sizes=sizes, dt=1e-3, steps=1)
+    assert_tree_equal(out, ref)
+    for key in ("interactions", "node_visits", "far_nodes", "far_interactions"):
+        assert out[key] == ref[key], (cfg, key)
+    ok, rel = acc_close(out["acc4"], ref["acc4"])
+    assert ok.all(), f"{cfg}: {(~ok).sum()} particles outside tolerance, worst {rel.max():.3e}"
