@@ -9,10 +9,10 @@
 //      last block turns the counts into exclusive digit offsets;
 //   2. one kernel per pass: each block takes the next tile (atomic ticket),
 //      ranks its keys stably with warp-ballot peer masks and per-warp digit
-//      counters in shared memory, publishes its digit counts, obtains the
-//      counts of all earlier tiles by decoupled look-back (bounded waits),
-//      and scatters through shared memory so that runs of one digit leave
-//      as contiguous stores.
+//      counters in shared memory, publishes its digit counts, stages the
+//      tile in sorted order in shared memory, obtains the counts of all
+//      earlier tiles by decoupled look-back (bounded waits), and writes each
+//      digit's run of the tile with contiguous stores.
 // A stable LSD sort yields the one stable permutation, so the result equals
 // the reference's bit by bit, including the order of equal keys.
 #include <algorithm>
