@@ -77,8 +77,13 @@ SIGNATURES = {
     "astro_radix_sort_temp_bytes": (c_int, [c_uint32, c_uint32, POINTER(c_size_t)]),
     "astro_radix_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p,
                                  c_uint32, c_void_p, c_size_t, c_void_p]),
+    "astro_radix_sort_status": (c_int, [c_void_p, c_void_p]),
     "astro_radix_sort_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32,
                                          c_void_p, c_uint32, c_void_p]),
+    "astro_radix_sort_noalloc_status": (c_int, [c_void_p]),
+    "astro_test_sort_lookback_timeout": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32,
+                                                 c_uint32, c_uint32, c_void_p, c_size_t,
+                                                 c_void_p]),
     "astro_generate_ic": (c_int, [c_uint32, c_uint64, c_uint32, c_uint32, c_double, c_double,
                                   c_void_p, c_void_p, c_void_p]),
     "astro_generate_system_sizes": (c_int, [c_uint64, c_uint32, c_uint32, c_uint32, c_double,

@@ -94,12 +94,15 @@ constexpr uint32_t kLbInclusive = 2u << 30;
 constexpr uint32_t kLbCountMask = (1u << 30) - 1;
 
 // Spin on the status word of an earlier tile until it is published, then
-// return it. Returns 0 after kSpinLimit polls and sets the error bit.
-__device__ __forceinline__ uint32_t lookback_wait(const uint32_t* word, uint32_t* err) {
+// return it. After `limit` polls it sets the error bit and returns an
+// inclusive zero, so the caller's prefix only misses counts (its stores stay
+// below their true positions, inside the output).
+__device__ __forceinline__ uint32_t lookback_wait(const uint32_t* word, uint32_t* err,
+                                                  uint32_t limit = kSpinLimit) {
     uint32_t v = ld_relaxed_u32(word);
     uint32_t polls = 0;
     while ((v >> 30) == 0) {
-        if (++polls > kSpinLimit) {
+        if (++polls > limit) {
             atomicOr(err, kErrLookbackTimeout);
             return kLbInclusive;  // treat as an inclusive zero so the caller stops
         }
@@ -117,7 +120,8 @@ __device__ __forceinline__ uint32_t lookback_wait(const uint32_t* word, uint32_t
 constexpr int kLbWindow = 8;
 __device__ __forceinline__ uint32_t lookback_window(const uint32_t* words, uint32_t tile,
                                                     uint32_t col, uint32_t* err,
-                                                    uint32_t stride = 256) {
+                                                    uint32_t stride = 256,
+                                                    uint32_t limit = kSpinLimit) {
     uint32_t prefix = 0;
     int64_t j = (int64_t)tile - 1;
     while (j >= 0) {
@@ -133,7 +137,7 @@ __device__ __forceinline__ uint32_t lookback_window(const uint32_t* words, uint3
         }
         j -= k;
         if (k < kLbWindow) {
-            const uint32_t w = lookback_wait(words + (size_t)j * stride + col, err);
+            const uint32_t w = lookback_wait(words + (size_t)j * stride + col, err, limit);
             prefix += w & kLbCountMask;
             if ((w & kLbInclusive) != 0) return prefix;
             --j;

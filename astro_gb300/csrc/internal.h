@@ -51,7 +51,7 @@ SortPlan sort_plan(uint32_t max_len, uint32_t key_bits);
 cudaError_t sort_init();
 // Stable sort of n_est (key, value) pairs (count read from d_count when not
 // NULL). vals_in NULL => values are 0..n-1. err (device word) collects
-// look-back timeouts; NULL => the word inside temp.
+// look-back timeouts; NULL => the error word inside temp (sort_status).
 // variant: 0 = the library default, 1..sort_variant_count() = a pass kernel
 // of the astro_params.sort_variant table.
 cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
@@ -59,6 +59,17 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
                        uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
                        uint32_t* err, uint32_t variant = 0);
 uint32_t sort_variant_count();
+// Test hook: a one-pass sort (key_bits <= 8) whose tile 0 is never
+// processed, so the look-back waits of the later tiles give up after
+// spin_limit polls and set the error word of `temp`.
+cudaError_t sort_pairs_stalled(const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out,
+                               uint32_t n, uint32_t key_bits, void* temp, size_t temp_bytes,
+                               uint32_t spin_limit, cudaStream_t st);
+// Waits for st, then reads and clears the error word of a sort scratch:
+// ASTRO_OK, ASTRO_ERR_DEVICE_TIMEOUT (a look-back wait gave up) or ASTRO_ERR_CUDA.
+int sort_status(const void* temp, cudaStream_t st);
+// The no-alloc sort's static scratch on the current device (sort_noalloc.cu).
+cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
 
 // ------------------------------------------------------------ pipeline ----
 struct DeviceState;  // defined in context.cu

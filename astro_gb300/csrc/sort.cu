@@ -17,6 +17,7 @@
 // the reference's bit by bit, including the order of equal keys.
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 
 #include "common.cuh"
 #include "internal.h"
@@ -158,7 +159,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
     const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
-    uint32_t digit_bits, uint32_t* __restrict__ err) {
+    uint32_t digit_bits, uint32_t* __restrict__ err, uint32_t spin_limit) {
     using Smem = PassSmem<kItems>;
     constexpr int kTile = Smem::kTile;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -245,7 +246,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     }
     uint32_t prefix = 0;
     if (tile > 0) {
-        prefix = lookback_window(lookback, tile, tid, err);
+        prefix = lookback_window(lookback, tile, tid, err, kRadix, spin_limit);
         st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
     }
     sm.global_base[tid] = excl[tid] + prefix;
@@ -293,9 +294,10 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 // Bounded wait for the phase of the given parity; false (and the error bit)
-// after kSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
-    for (uint32_t polls = 0; polls < kSpinLimit; ++polls) {
+// after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err,
+                                          uint32_t limit) {
+    for (uint32_t polls = 0; polls < limit; ++polls) {
         if (mbar_test(bar, parity)) return true;
         if (polls > 64) __nanosleep(32);
     }
@@ -330,7 +332,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kern
     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
     const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
-    uint32_t digit_bits, uint32_t* __restrict__ err) {
+    uint32_t digit_bits, uint32_t* __restrict__ err, uint32_t spin_limit) {
     using Smem = PipeSmem<kItems>;
     constexpr int kTile = Smem::kTile;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -382,7 +384,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kern
         uint64_t key[kItems];
         uint32_t val[kItems], pos[kItems];
         if ((pending >> b) & 1u) {
-            mbar_wait(&sm.bar[b], (phase >> b) & 1u, err);
+            mbar_wait(&sm.bar[b], (phase >> b) & 1u, err, spin_limit);
             phase ^= 1u << b;
             pending &= ~(1u << b);
 #pragma unroll
@@ -429,7 +431,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kern
         sm.tile_start[tid] = tile_start;
         uint32_t prefix = 0;
         if (cur > 0) {
-            prefix = lookback_window(lookback, cur, tid, err);
+            prefix = lookback_window(lookback, cur, tid, err, kRadix, spin_limit);
             st_relaxed_u32(my_word, kLbInclusive | (prefix + tile_cnt));
         }
         sm.global_base[tid] = excl[tid] + prefix;
@@ -466,7 +468,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kern
     // A copy is only left in flight if a wait gave up; wait for it (bounded)
     // before the block's shared memory is released.
     for (uint32_t k = 0; k < 2; ++k)
-        if ((pending >> k) & 1u) mbar_wait(&sm.bar[k], (phase >> k) & 1u, err);
+        if ((pending >> k) & 1u) mbar_wait(&sm.bar[k], (phase >> k) & 1u, err, spin_limit);
 }
 
 // Pass-kernel variants (items per thread, blocks per SM, ranking; the
@@ -474,7 +476,7 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_pipelined_kern
 struct PassVariant {
     int items;
     void (*kernel)(const uint64_t*, const uint32_t*, uint64_t*, uint32_t*, const uint32_t*, uint32_t,
-                   const uint32_t*, uint32_t*, uint32_t*, uint32_t, uint32_t, uint32_t*);
+                   const uint32_t*, uint32_t*, uint32_t*, uint32_t, uint32_t, uint32_t*, uint32_t);
     size_t smem;
     bool pipelined;
 };
@@ -495,26 +497,46 @@ constexpr int kMinItems = 8;  // sizes the look-back words for every variant
 static_assert(kThreads * kMinItems == (int)kSortPlanTile, "look-back sizing");
 int g_variant = 5;
 
-int g_num_sms = 0;
+// Per-device set-up state: the pass kernels' shared-memory attribute is set
+// once on each device that sorts, and the SM count is cached per device.
+constexpr int kMaxDevices = 64;
+bool g_init_done[kMaxDevices] = {};
+int g_num_sms[kMaxDevices] = {};
+std::mutex g_init_mutex;
+
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 0;
+    return dev;
+}
 
 int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 1;
+    const int dev = current_device();
+    std::lock_guard<std::mutex> lock(g_init_mutex);
+    if (g_num_sms[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        g_num_sms[dev] = n > 0 ? n : 1;
     }
-    return g_num_sms;
+    return g_num_sms[dev];
 }
+
+// Position of the error word inside the scratch (the counters come first,
+// so the word sits at the same offset for every length and key width).
+constexpr size_t kErrWord = 9;
 
 }  // namespace
 
-// One-time kernel attribute (the pass kernel's shared memory exceeds the
-// 48 KB default). Safe to call repeatedly; called before any stream capture.
+// Kernel attributes (the pass kernels' shared memory exceeds the 48 KB
+// default), set once per device. Safe to call repeatedly and from several
+// threads; called before any stream capture.
 cudaError_t sort_init() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_init_mutex);
+    if (g_init_done[dev]) return cudaSuccess;
     for (int v = 0; v < kNumVariants; ++v) {
         e = cudaFuncSetAttribute(kVariants[v].kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kVariants[v].smem);
@@ -527,7 +549,7 @@ cudaError_t sort_init() {
     }
     e = cudaFuncSetAttribute(sort_histogram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(kWarps * kMaxPasses * kRadix * sizeof(uint32_t)));
-    if (e == cudaSuccess) done = true;
+    if (e == cudaSuccess) g_init_done[dev] = true;
     return e;
 }
 
@@ -539,38 +561,51 @@ SortPlan sort_plan(uint32_t max_len, uint32_t key_bits) {
     p.tile = kSortPlanTile;
     p.ntiles = (uint32_t)(((uint64_t)max_len + p.tile - 1) / p.tile);
     size_t off = 0;
+    // Zeroed at the start of every sort: counters ([0..7] tile tickets per
+    // pass, [8] histogram blocks done, [9] error word), histograms and
+    // look-back words.
+    p.zero_begin = off;
+    p.counters = off;
+    off = align_up(off + 4ull * 16, 256);
+    p.hist = off;
+    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
+    p.lookback = off;
+    off = align_up(off + 4ull * p.passes * (size_t)std::max(p.ntiles, 1u) * kRadix, 256);
+    p.zero_end = off;
+    p.excl = off;
+    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
     p.keys_tmp = off;
     off = align_up(off + 8ull * max_len, 256);
     p.vals_tmp = off;
     off = align_up(off + 4ull * max_len, 256);
-    p.excl = off;
-    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
-    p.zero_begin = off;
-    p.hist = off;
-    off = align_up(off + 4ull * kMaxPasses * kRadix, 256);
-    p.counters = off;  // [0..7] tile tickets per pass, [8] histogram blocks done, [9] error
-    off = align_up(off + 4ull * 16, 256);
-    p.lookback = off;
-    off = align_up(off + 4ull * p.passes * (size_t)std::max(p.ntiles, 1u) * kRadix, 256);
-    p.zero_end = off;
     p.total = off;
     return p;
 }
 
-cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
-                       uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
-                       uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
-                       uint32_t* err, uint32_t variant) {
+namespace {
+
+// The sort's kernels on the scratch `temp` (laid out by sort_plan). With
+// `stall_first_tile` (test hook, one pass only) the first pass hands out
+// tickets from 1, so tile 0 is never processed and every later tile's
+// look-back waits on a word that nobody publishes until `spin_limit` polls.
+cudaError_t sort_launch(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                        uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
+                        uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
+                        uint32_t* err, uint32_t variant, uint32_t spin_limit,
+                        bool stall_first_tile) {
     if (n_est == 0) return cudaSuccess;
     const SortPlan plan = sort_plan(n_est, key_bits);
     if (temp_bytes < plan.total || key_bits > 64 || variant > (uint32_t)kNumVariants)
         return cudaErrorInvalidValue;
+    if (stall_first_tile && plan.passes != 1) return cudaErrorInvalidValue;
     cudaError_t e0 = sort_init();
     if (e0 != cudaSuccess) return e0;
     int vi = variant == 0 ? g_variant : (int)variant - 1;
     // Bulk copies need 16-byte aligned sources; the temporaries always are.
+    // The stalled test pass needs one block per tile (no persistent blocks).
     if (kVariants[vi].pipelined &&
-        (((uintptr_t)keys_in | (uintptr_t)(vals_in ? vals_in : nullptr)) & 15u) != 0)
+        (stall_first_tile ||
+         (((uintptr_t)keys_in | (uintptr_t)(vals_in ? vals_in : nullptr)) & 15u) != 0))
         vi = kFallbackVariant;
     const PassVariant& pv = kVariants[vi];
     const uint32_t tile = (uint32_t)(kThreads * pv.items);
@@ -590,9 +625,14 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
     uint32_t* hist = reinterpret_cast<uint32_t*>(base + plan.hist);
     uint32_t* counters = reinterpret_cast<uint32_t*>(base + plan.counters);
     uint32_t* lookback = reinterpret_cast<uint32_t*>(base + plan.lookback);
-    if (!err) err = counters + 9;
+    if (!err) err = counters + kErrWord;
     cudaError_t e = cudaMemsetAsync(base + plan.zero_begin, 0, plan.zero_end - plan.zero_begin, st);
     if (e != cudaSuccess) return e;
+    if (stall_first_tile) {
+        // Pass 0's ticket counter starts at 1 (its low byte set to 1).
+        e = cudaMemsetAsync(counters, 1, 1, st);
+        if (e != cudaSuccess) return e;
+    }
     const uint32_t hist_blocks = (uint32_t)std::min<uint64_t>(
         ((uint64_t)n_est + 4 * kThreads - 1) / (4 * kThreads), (uint64_t)num_sms() * kHistBlocksPerSm);
     const size_t hist_smem = (size_t)kWarps * plan.passes * kRadix * sizeof(uint32_t);
@@ -608,11 +648,49 @@ cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_
         const uint32_t bits = key_bits == 0 ? 0u : std::min(8u, key_bits - shift);
         pv.kernel<<<grid, kThreads, pv.smem, st>>>(
             kin, vin, kout, vout, d_count, n_est, excl + p * kRadix,
-            lookback + (size_t)p * plan.ntiles * kRadix, counters + p, shift, bits, err);
+            lookback + (size_t)p * plan.ntiles * kRadix, counters + p, shift, bits, err, spin_limit);
         kin = kout;
         vin = vout;
     }
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t sort_pairs(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                       uint32_t* vals_out, uint32_t n_est, const uint32_t* d_count,
+                       uint32_t key_bits, void* temp, size_t temp_bytes, cudaStream_t st,
+                       uint32_t* err, uint32_t variant) {
+    return sort_launch(keys_in, vals_in, keys_out, vals_out, n_est, d_count, key_bits, temp,
+                       temp_bytes, st, err, variant, kSpinLimit, false);
+}
+
+cudaError_t sort_pairs_stalled(const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out,
+                               uint32_t n, uint32_t key_bits, void* temp, size_t temp_bytes,
+                               uint32_t spin_limit, cudaStream_t st) {
+    return sort_launch(keys_in, nullptr, keys_out, vals_out, n, nullptr, key_bits, temp, temp_bytes,
+                       st, nullptr, 0, spin_limit, true);
+}
+
+int sort_status(const void* temp, cudaStream_t st) {
+    if (!temp) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    uint32_t* word = reinterpret_cast<uint32_t*>(static_cast<char*>(const_cast<void*>(temp)) +
+                                                 sort_plan(0, 8).counters) + kErrWord;
+    uint32_t v = 0;
+    if (cudaMemcpy(&v, word, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    if (v == 0) return ASTRO_OK;
+    if (cudaMemset(word, 0, sizeof(uint32_t)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    return (v & kErrLookbackTimeout) ? ASTRO_ERR_DEVICE_TIMEOUT : ASTRO_ERR_DEVICE_OVERFLOW;
 }
 
 }  // namespace astro
@@ -626,6 +704,8 @@ extern "C" int astro_radix_sort_temp_bytes(uint32_t max_length, uint32_t key_bit
 // MetalKernelsRadixSort.sort (Astro/RadixSort.swift:98-105): input/inputIndices
 // are read, output/outputIndices receive the sorted pairs, estimatedLength
 // sizes the launch and actualCountBuffer (d_actual_count) holds the count.
+// On the NULL stream the call waits for the sort and returns its device
+// status; on any other stream astro_radix_sort_status reads it later.
 extern "C" int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
                                 uint64_t* d_output, uint32_t* d_output_indices,
                                 uint32_t estimated_length, const uint32_t* d_actual_count,
@@ -637,8 +717,39 @@ extern "C" int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input
         (const void*)d_input_indices == (const void*)d_output_indices)
         return ASTRO_ERR_INVALID_ARGUMENT;
     if (temp_bytes < astro::sort_plan(estimated_length, key_bits).total) return ASTRO_ERR_CAPACITY;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = astro::sort_pairs(d_input, d_input_indices, d_output, d_output_indices,
                                       estimated_length, d_actual_count, key_bits, d_temp,
-                                      temp_bytes, static_cast<cudaStream_t>(stream), nullptr);
-    return e == cudaSuccess ? ASTRO_OK : ASTRO_ERR_CUDA;
+                                      temp_bytes, st, nullptr);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    return st == nullptr ? astro::sort_status(d_temp, st) : ASTRO_OK;
+}
+
+extern "C" int astro_radix_sort_status(const void* d_temp, void* stream) {
+    return astro::sort_status(d_temp, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int astro_test_sort_lookback_timeout(const uint64_t* d_input, uint64_t* d_output,
+                                                uint32_t* d_output_indices, uint32_t n,
+                                                uint32_t key_bits, uint32_t spin_limit,
+                                                void* d_temp, size_t temp_bytes, void* stream) {
+    if (!d_input || !d_output || !d_output_indices || n == 0 || key_bits == 0 || key_bits > 8 ||
+        spin_limit == 0 || spin_limit > astro::kSpinLimit)
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    if ((const void*)d_input == (const void*)d_output) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!d_temp && astro::noalloc_scratch(&d_temp, &temp_bytes) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    if (temp_bytes < astro::sort_plan(n, key_bits).total) return ASTRO_ERR_CAPACITY;
+    cudaError_t e = astro::sort_pairs_stalled(d_input, d_output, d_output_indices, n, key_bits, d_temp,
+                                              temp_bytes, spin_limit, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    return ASTRO_OK;
 }

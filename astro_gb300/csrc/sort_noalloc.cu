@@ -27,9 +27,10 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxLength = ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH;
 
-// Bytes of sort_plan(kNoAllocMaxLength, 64): ping-pong keys (8 B) and values
-// (4 B), 8 passes of 256-bin offsets and histograms, the counters and 8
-// passes of 256 look-back words per tile, each region 256-aligned.
+// Bytes of sort_plan(kNoAllocMaxLength, 64): the counters (error word
+// included), 8 passes of 256-bin histograms, 8 passes of 256 look-back
+// words per tile, 8 passes of 256-bin offsets and the ping-pong keys (8 B)
+// and values (4 B), each region 256-aligned.
 constexpr size_t kTiles = (kNoAllocMaxLength + astro::kSortPlanTile - 1) / astro::kSortPlanTile;
 constexpr size_t kNoAllocBytes = 8ull * kNoAllocMaxLength + 4ull * kNoAllocMaxLength +
                                  4ull * 8 * 256 + 4ull * 8 * 256 + 256 + 4ull * 8 * kTiles * 256;
@@ -59,6 +60,14 @@ cudaError_t scratch_address(void** out) {
 
 }  // namespace
 
+namespace astro {
+// The static scratch of this device and its size (for the test hook).
+cudaError_t noalloc_scratch(void** ptr, size_t* bytes) {
+    *bytes = kNoAllocBytes;
+    return scratch_address(ptr);
+}
+}  // namespace astro
+
 // No counterpart in the reference: astro_radix_sort with the scratch in a
 // static device array instead of caller-supplied memory.
 extern "C" int astro_radix_sort_noalloc(const uint64_t* d_input, const uint32_t* d_input_indices,
@@ -79,8 +88,27 @@ extern "C" int astro_radix_sort_noalloc(const uint64_t* d_input, const uint32_t*
         (void)cudaGetLastError();
         return ASTRO_ERR_CUDA;
     }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = astro::sort_pairs(d_input, d_input_indices, d_output, d_output_indices,
                                       estimated_length, d_actual_count, key_bits, scratch,
-                                      kNoAllocBytes, static_cast<cudaStream_t>(stream), nullptr);
-    return e == cudaSuccess ? ASTRO_OK : ASTRO_ERR_CUDA;
+                                      kNoAllocBytes, st, nullptr);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    // On the NULL stream the call waits and reports the sort's device status
+    // (a look-back wait that gave up); otherwise the caller reads it with
+    // astro_radix_sort_noalloc_status once the stream has reached this sort.
+    return st == nullptr ? astro::sort_status(scratch, st) : ASTRO_OK;
+}
+
+// The device status of the last no-alloc sort on the current device: waits
+// for `stream`, then reads and clears the error word in the static array.
+extern "C" int astro_radix_sort_noalloc_status(void* stream) {
+    void* scratch = nullptr;
+    if (scratch_address(&scratch) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ASTRO_ERR_CUDA;
+    }
+    return astro::sort_status(scratch, static_cast<cudaStream_t>(stream));
 }

@@ -34,3 +34,9 @@ class RadixSort:
         check(lib().astro_radix_sort(ptr(input), ptr(input_indices), ptr(output),
                                      ptr(output_indices), estimated_length, ptr(actual_count),
                                      self.key_bits, ptr(self.temp), self.temp.numel(), stream))
+
+    def status(self, stream: int = 0) -> None:
+        """Wait for `stream` and raise AstroError(ASTRO_ERR_DEVICE_TIMEOUT) if
+        the last sort on this sorter's temporaries had a look-back wait give
+        up (the NULL stream's sort already reported it from sort())."""
+        check(lib().astro_radix_sort_status(ptr(self.temp), stream))

@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2",
                     help="c1..c5: PHYSICAL workloads; ref: the reference's own scene")
     ap.add_argument("--form", choices=["plain", "precision"], default="plain")
+    ap.add_argument("--n", type=int, default=None,
+                    help="particles of a single-system workload (smaller cases for profiling)")
     # Launch knobs: unset ones come from the autotuner's file for the
     # workload and form (astro_gb300/tuned.json), else the preset defaults.
     ap.add_argument("--lbits", type=int, default=None)
@@ -94,6 +96,18 @@ def parse():
     ap.add_argument("--one-at-a-time", action="store_true",
                     help="batched workload: also time the systems stepped one at a time")
     return ap.parse_args()
+
+
+def workload(args):
+    """The workload of --workload, with --n particles when given."""
+    import dataclasses
+
+    w = WORKLOADS[args.workload]
+    if args.n is not None:
+        if w.generator in ("batch", "reference_scene"):
+            raise SystemExit("--n applies to the single-system PHYSICAL workloads")
+        w = dataclasses.replace(w, n=args.n)
+    return w
 
 
 CLIMB_MIN_NODES = 32768  # build.cu: layers of at least this capacity get a launch each
@@ -150,7 +164,7 @@ def knobs(args):
 
 
 def make_params(args, ag, L):
-    w = WORKLOADS[args.workload]
+    w = workload(args)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     k, source = knobs(args)
     if w.preset == "reference":
@@ -333,7 +347,7 @@ def run_ours(args, world, rank, local):
     from astro_gb300 import layouts as L
 
     torch.cuda.set_device(local)
-    w = WORKLOADS[args.workload]
+    w = workload(args)
     desc, dt = w.description, w.dt
     pm, vr, sizes = w.make()
     n = len(pm)
@@ -564,7 +578,7 @@ def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
     cores = orc.set_threads(args.cpu_threads)
     steps, t_total = 0, 0.0
     pm_c, vr_c = pm.copy(), vr.copy()
-    w = WORKLOADS[args.workload]
+    w = workload(args)
     while True:
         t0 = time.perf_counter()
         cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
@@ -583,7 +597,7 @@ def run_reference(args):
     from astro_gb300 import layouts as L
     from oracle import oracle as orc
 
-    w = WORKLOADS[args.workload]
+    w = workload(args)
     desc, dt = w.description, w.dt
     pm, vr, sizes = w.make()
     n = len(pm)

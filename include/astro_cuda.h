@@ -397,6 +397,13 @@ const char* astro_status_string(int status);
  * (key_bits = 64 reproduces the reference's 64 one-bit passes exactly;
  * fewer bits give the same permutation when the high bits are zero).
  * Temporary device memory is supplied by the caller.
+ *
+ * Device status: the sort's look-back waits are bounded; a wait that gives
+ * up (ASTRO_ERR_DEVICE_TIMEOUT) leaves a wrong permutation, written inside
+ * the output. On the NULL stream astro_radix_sort waits for the sort and
+ * returns that status. On any other stream it returns once the sort is
+ * queued; astro_radix_sort_status then waits for the stream and returns the
+ * status of the last sort that used d_temp (and clears it).
  * ------------------------------------------------------------------------- */
 int astro_radix_sort_temp_bytes(uint32_t max_length, uint32_t key_bits, size_t* bytes);
 int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
@@ -404,6 +411,10 @@ int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
                      uint32_t estimated_length, const uint32_t* d_actual_count,
                      uint32_t key_bits, void* d_temp, size_t temp_bytes,
                      void* stream);
+/* No counterpart in the reference (its sort reports nothing): ASTRO_OK or
+ * ASTRO_ERR_DEVICE_TIMEOUT for the last sort made with d_temp, after
+ * waiting for stream. */
+int astro_radix_sort_status(const void* d_temp, void* stream);
 
 /* ---------------------------------------------------------------------------
  * The same sort for callers that cannot allocate device memory (no
@@ -416,13 +427,17 @@ int astro_radix_sort(const uint64_t* d_input, const uint32_t* d_input_indices,
  * loads the library holds the array (about 16 MiB) until exit. All calls on a
  * device share the array: calls that overlap on the GPU race, so serialise
  * them. The first call on a device resolves the array's address there; make
- * it before any stream capture begins.
+ * it before any stream capture begins. Device status as astro_radix_sort:
+ * returned by the call itself on the NULL stream, otherwise by
+ * astro_radix_sort_noalloc_status (the last no-alloc sort on the current
+ * device, after waiting for stream).
  * ------------------------------------------------------------------------- */
 #define ASTRO_RADIX_SORT_NOALLOC_MAX_LENGTH 1048576u
 int astro_radix_sort_noalloc(const uint64_t* d_input, const uint32_t* d_input_indices,
                              uint64_t* d_output, uint32_t* d_output_indices,
                              uint32_t estimated_length, const uint32_t* d_actual_count,
                              uint32_t key_bits, void* stream);
+int astro_radix_sort_noalloc_status(void* stream);
 
 /* ---------------------------------------------------------------------------
  * Seeded initial conditions (host side, FP64 then cast). Counter-based
