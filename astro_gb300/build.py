@@ -21,8 +21,8 @@ OBJ_DIR = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-SOURCES = ["sort.cu", "sort_noalloc.cu", "build.cu", "traverse.cu", "splat.cu", "context.cu",
-           "tune.cu", "ic.cpp"]
+SOURCES = ["sort.cu", "sort_noalloc.cu", "build.cu", "traverse.cu", "traverse_group.cu", "splat.cu",
+           "context.cu", "tune.cu", "ic.cpp"]
 
 
 def nvcc() -> str:
@@ -35,6 +35,12 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: set CUDA_HOME or put nvcc on PATH")
 
 
+def extra_flags() -> list:
+    """Additional nvcc flags from ASTRO_NVCC_FLAGS (space-separated), for
+    builds with other compile-time tuning constants."""
+    return os.environ.get("ASTRO_NVCC_FLAGS", "").split()
+
+
 def _compile(src: str, verbose_ptxas: bool) -> Path:
     obj = OBJ_DIR / (src + ".o")
     s = CSRC / src
@@ -42,7 +48,7 @@ def _compile(src: str, verbose_ptxas: bool) -> Path:
         cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", "-c", str(s), "-o", str(obj)]
     else:
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(s), "-o", str(obj)]
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra_flags(), "-c", str(s), "-o", str(obj)]
         if verbose_ptxas:
             cmd += ["-Xptxas", "-v"]
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -59,7 +65,7 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
     LIB_DIR.mkdir(exist_ok=True)
     deps = sorted(CSRC.glob("*")) + [PKG.parent / "include" / "astro_cuda.h"]
     newest = max(p.stat().st_mtime for p in deps)
-    if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
+    if LIB.exists() and not force and not extra_flags() and LIB.stat().st_mtime >= newest:
         return LIB
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))

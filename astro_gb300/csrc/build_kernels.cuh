@@ -55,7 +55,8 @@ struct AggArgs {
     uint32_t* err;         // device error word (kErrBadLayer: a node with > 8 children)
 };
 
-constexpr uint32_t kGroupSize = 32;  // largest group of the group walk (one warp)
+constexpr uint32_t kGroupSize = 64;     // largest group of the group walk (two particles per lane)
+constexpr uint32_t kDefaultGroupSize = 32;  // group_size 0
 constexpr uint32_t kNoParent = 0xFFFFFFFFu;
 
 struct DirectArgs {
@@ -69,6 +70,21 @@ struct DirectArgs {
     uint32_t n_sample;
     double g;
     double eps2;
+};
+
+// The lists of one group of the group walk, written by the walk kernel and
+// read by the evaluation kernel. Each list is a chain of blocks of
+// kListBlockWords words of the list pool (block b at lists[b * kListBlockWords],
+// the next block of the chain in list_next[b]): accepted node ids (cells,
+// far nodes) one word each, leaf particle ranges two words each. Also the
+// centre of the group's bounding box (the far nodes' expansion point).
+constexpr uint32_t kListBlockWords = 64;
+struct GroupDesc {
+    uint32_t leaf_first, n_leaf;
+    uint32_t cell_first, n_cell;
+    uint32_t far_first, n_far;
+    float gcx, gcy, gcz;
+    uint32_t pad[3];
 };
 
 struct TraverseArgs {
@@ -112,8 +128,15 @@ struct TraverseArgs {
     const float* node_qyz;
     const uint2* groups;
     const uint32_t* group_count;
-    uint32_t* frontier;       // per-warp ping-pong buffers, 2 * frontier_cap each
+    uint32_t* frontier;       // group walk: per-warp frontier ping-pong buffers,
+                              // 2 * frontier_cap words each
     uint32_t frontier_cap;
+    GroupDesc* desc;          // group walk: per group, its lists in the pool and centre
+    uint32_t* lists;          // group walk: list pool, lists_blocks blocks
+    uint32_t* list_next;      // group walk: next block of each block's chain
+    uint32_t lists_blocks;    // pool size in blocks
+    uint32_t* lists_used;     // pool bump counter (blocks handed out)
+    uint32_t* eval_queue;     // queue of the group evaluation kernel
     uint32_t nsys;
     float far2;               // group walk: far_ratio^2 (0: no far nodes)
     uint32_t group_chunk;     // group walk: groups visited in scrambled chunks of this
@@ -209,9 +232,12 @@ struct TraverseConfig {
 };
 cudaError_t launch_traverse_ref(const TraverseArgs& a, cudaStream_t st);
 cudaError_t launch_traverse_phys(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
-// Group walk: warps resident in the persistent launch (sizes the frontier
-// scratch) and the launch itself.
-uint32_t group_walk_warps(const TraverseConfig& c);
+// Group walk: warps of the persistent walk launch (each owns two frontier
+// buffers of frontier_cap words), the list pool size in blocks for n
+// particles in groups of at most group_size, and the two launches (walk,
+// then evaluation).
+uint32_t group_walk_warps();
+size_t group_list_blocks(uint32_t n, uint32_t group_size);
 cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
 
 }  // namespace astro

@@ -88,7 +88,8 @@ int validate_params(const astro_params* p, const char** why) {
         return (*why = "g and softening must be finite, softening >= 0", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->block_warps != 0 && p->block_warps != 2 && p->block_warps != 4 && p->block_warps != 8)
         return (*why = "block_warps must be 0, 2, 4 or 8", ASTRO_ERR_INVALID_ARGUMENT);
-    if (p->group_size > 32) return (*why = "group_size must be in [0, 32]", ASTRO_ERR_INVALID_ARGUMENT);
+    if (p->group_size > astro::kGroupSize)
+        return (*why = "group_size must be in [0, 64]", ASTRO_ERR_INVALID_ARGUMENT);
     if (p->sort_variant > astro::sort_variant_count())
         return (*why = "unknown sort_variant", ASTRO_ERR_INVALID_ARGUMENT);
     if (!(p->open_delta_weight >= 0.0f) || !std::isfinite(p->open_delta_weight))
@@ -169,7 +170,8 @@ int check_device(astro_ctx* ctx) {
         if (err & astro::kErrLookbackTimeout)
             return fail(ctx, ASTRO_ERR_DEVICE_TIMEOUT, "a decoupled look-back wait gave up");
         if (err & astro::kErrFrontier)
-            return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW, "a group walk frontier exceeded its buffer");
+            return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW,
+                        "a group walk buffer (frontier or list pool) overflowed");
         return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW, "a traversal stack bound was hit");
     }
     return ASTRO_OK;
@@ -203,19 +205,29 @@ bool group_walk(const astro_ctx* ctx) {
     return is_phys(ctx) && (ctx->p.flags & ASTRO_FLAG_PER_PARTICLE) == 0;
 }
 
-// Frontier scratch of the group walk: two buffers of frontier_cap node
-// indices per resident warp of the persistent launch, and a third for the
-// far-node list when params.far_ratio > 0.
+// Buffers of the group walk: two frontier buffers of frontier_cap words per
+// warp of the persistent walk launch; the list pool (blocks and their chain
+// links, sized for max_n); one descriptor per group (at most max_n groups).
 int ensure_frontier(astro_ctx* ctx) {
     if (!group_walk(ctx)) return ASTRO_OK;
-    astro::TraverseConfig c = traverse_config(ctx);
-    const size_t per_warp = ctx->p.far_ratio > 0.0f ? 3 : 2;
-    const size_t words = (size_t)astro::group_walk_warps(c) * per_warp * ctx->frontier_cap;
-    if (words <= ctx->frontier_words) return ASTRO_OK;
-    dev_free(ctx->frontier);
-    ctx->frontier_words = 0;
-    CK(dev_alloc(&ctx->frontier, words));
-    ctx->frontier_words = words;
+    const size_t words = (size_t)astro::group_walk_warps() * 2 * ctx->frontier_cap;
+    if (words > ctx->frontier_words) {
+        dev_free(ctx->frontier);
+        ctx->frontier_words = 0;
+        CK(dev_alloc(&ctx->frontier, words));
+        ctx->frontier_words = words;
+    }
+    const size_t blocks = astro::group_list_blocks(
+        ctx->max_n, ctx->p.group_size ? ctx->p.group_size : astro::kDefaultGroupSize);
+    if (blocks > ctx->lists_blocks) {
+        dev_free(ctx->lists);
+        dev_free(ctx->list_next);
+        ctx->lists_blocks = 0;
+        CK(dev_alloc(&ctx->lists, blocks * astro::kListBlockWords));
+        CK(dev_alloc(&ctx->list_next, blocks));
+        ctx->lists_blocks = blocks;
+    }
+    if (!ctx->group_desc) CK(dev_alloc(&ctx->group_desc, ctx->max_n));
     return ASTRO_OK;
 }
 
@@ -302,7 +314,7 @@ int stage_build(astro_ctx* ctx) {
     a.want_delta = (ctx->p.flags & ASTRO_FLAG_OPEN_DELTA) ? 1u : 0u;
     a.theta = ctx->p.theta;
     a.delta_weight = ctx->p.open_delta_weight;
-    a.group_size = ctx->p.group_size ? ctx->p.group_size : astro::kGroupSize;
+    a.group_size = ctx->p.group_size ? ctx->p.group_size : astro::kDefaultGroupSize;
     a.err = ctx->err;
     CK(cudaMemsetAsync(ctx->counters + 2, 0, sizeof(uint32_t), st));
     const uint32_t l0 = astro::climb_first_layer(ctx->layers);
@@ -354,6 +366,12 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     a.group_count = ctx->counters + 2;
     a.frontier = ctx->frontier;
     a.frontier_cap = ctx->frontier_cap;
+    a.desc = ctx->group_desc;
+    a.lists = ctx->lists;
+    a.list_next = ctx->list_next;
+    a.lists_blocks = (uint32_t)ctx->lists_blocks;
+    a.eval_queue = ctx->counters + 3;
+    a.lists_used = ctx->counters + 4;
     a.nsys = ctx->nsys;
     if (is_phys(ctx)) {
         a.eps2 = ctx->p.softening * ctx->p.softening;
@@ -627,6 +645,9 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->node_qyz);
     dev_free(ctx->groups);
     dev_free(ctx->frontier);
+    dev_free(ctx->lists);
+    dev_free(ctx->list_next);
+    dev_free(ctx->group_desc);
     if (ctx->readback) cudaFree(ctx->readback);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -73,6 +73,7 @@ cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
 
 // ------------------------------------------------------------ pipeline ----
 struct DeviceState;  // defined in context.cu
+struct GroupDesc;    // build_kernels.cuh
 
 }  // namespace astro
 
@@ -139,6 +140,10 @@ struct astro_ctx {
     uint32_t* frontier = nullptr;     // group-walk per-warp frontier buffers
     size_t frontier_words = 0;
     uint32_t frontier_cap = 16384;
+    astro::GroupDesc* group_desc = nullptr;  // group walk: per-group lists (<= max_n groups)
+    uint32_t* lists = nullptr;        // group walk: list pool
+    uint32_t* list_next = nullptr;    // group walk: block chain links
+    size_t lists_blocks = 0;
     uint32_t* layer_count = nullptr;  // device [ASTRO_MAX_LAYERS]
 
     // Systems.

@@ -171,8 +171,8 @@ typedef struct astro_params {
                                  (0 = only at layer 0) */
     uint32_t block_warps;     /* traversal: warps per block (0 = autotuned/default) */
     uint32_t group_size;      /* PHYSICAL group walk: at most this many consecutive
-                                 particles share one tree walk (one warp), 1..32;
-                                 0 = 32 */
+                                 particles share one tree walk (one warp; two
+                                 particles per lane above 32), 1..64; 0 = 32 */
     uint32_t sort_variant;    /* radix sort pass kernel (items per thread / blocks
                                  per SM / ranking): 0 = library default,
                                  1 = 16/2/ballot, 2 = 16/2/match, 3 = 12/3/match,

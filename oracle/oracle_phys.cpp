@@ -334,7 +334,8 @@ struct PhysState {
     static constexpr uint32_t kFlagDelta = 0x8u;      // ASTRO_FLAG_OPEN_DELTA
     static constexpr uint32_t kFlagQuad = 0x10u;      // ASTRO_FLAG_QUADRUPOLE
     static constexpr uint32_t kFlagPerParticle = 0x20u;  // ASTRO_FLAG_PER_PARTICLE
-    static constexpr uint32_t kGroupMax = 32;         // largest group (one warp)
+    static constexpr uint32_t kLanes = 32;            // far-node partials (one per lane of a warp)
+    static constexpr uint32_t kDefaultGroup = 32;     // group size of params.group_size = 0
 
     // One accumulator (plain or Kahan) per component.
     struct Acc {
@@ -556,13 +557,13 @@ struct PhysState {
 
     // Groups for the group walk: every particle in exactly one group of at
     // most kGroup consecutive (sorted) particles of one system, kGroup =
-    // params.group_size (0 = 32).
+    // params.group_size (0 = 32; at most 64, two particles per lane).
     //  - a node with more than kGroup particles packs its consecutive small
     //    children (at most kGroup particles each) greedily, in child order;
     //  - a top-layer node with at most kGroup particles is a group;
     //  - a leaf with more than kGroup particles is cut into kGroup chunks.
     std::vector<std::pair<uint32_t, uint32_t>> make_groups() const {
-        const uint32_t kGroup = p.group_size ? p.group_size : kGroupMax;
+        const uint32_t kGroup = p.group_size ? p.group_size : kDefaultGroup;
         std::vector<std::pair<uint32_t, uint32_t>> groups;
         for (uint32_t l = 0; l < layers; ++l)
             for (uint32_t k = 0; k < counts[l]; ++k) {
@@ -663,16 +664,16 @@ struct PhysState {
             }
             float fsum[kFarCoefs] = {};
             if (!far.empty()) {
-                float part[kGroupMax][kFarCoefs] = {};
+                float part[kLanes][kFarCoefs] = {};
                 static const float kZeroQ[5] = {0, 0, 0, 0, 0};
                 for (size_t f = 0; f < far.size(); ++f) {
                     float co[kFarCoefs];
                     far_coefs(&cm[4ull * far[f]], quad_on ? &quad[5ull * far[f]] : kZeroQ, gc, co);
-                    for (int k = 0; k < kFarCoefs; ++k) part[f % kGroupMax][k] += co[k];
+                    for (int k = 0; k < kFarCoefs; ++k) part[f % kLanes][k] += co[k];
                 }
-                for (uint32_t o = kGroupMax / 2; o > 0; o >>= 1) {
-                    float nxt[kGroupMax][kFarCoefs];
-                    for (uint32_t l = 0; l < kGroupMax; ++l)
+                for (uint32_t o = kLanes / 2; o > 0; o >>= 1) {
+                    float nxt[kLanes][kFarCoefs];
+                    for (uint32_t l = 0; l < kLanes; ++l)
                         for (int k = 0; k < kFarCoefs; ++k) nxt[l][k] = part[l][k] + part[l ^ o][k];
                     std::memcpy(part, nxt, sizeof(part));
                 }

@@ -129,7 +129,7 @@ def test_argument_errors_without_device(native):
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(theta=-1.0)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
-    bad = p.replace(group_size=33)
+    bad = p.replace(group_size=65)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(sort_variant=10)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
