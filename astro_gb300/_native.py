@@ -60,9 +60,11 @@ SIGNATURES = {
     "astro_read_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64),
                                  POINTER(c_uint64)]),
     "astro_read_far_stats": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
+    "astro_read_traverse_times": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float)]),
     "astro_step_batched": (c_int, [c_void_p, c_void_p, c_uint32, c_float, c_uint32]),
     "astro_autotune": (c_int, [c_void_p, c_char_p]),
     "astro_autotune_ex": (c_int, [c_void_p, c_char_p, c_float, c_uint32]),
+    "astro_autotune_keep": (c_int, [c_void_p, c_char_p, c_float, c_uint32, c_uint32]),
     "astro_direct_accel_f64": (c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
     "astro_lighting": (c_int, [c_void_p, c_uint32]),
     "astro_splat": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),

@@ -8,8 +8,8 @@ The knobs are fields of astro_params that change speed, not physics:
 
   block_warps   traversal block size (warps per block: 4 or 8)
   group_size    particles per warp: consecutive sorted particles sharing one
-                tree walk (1..32; groups of <= 16 run as several copies that
-                split the source lists)
+                tree walk (1..64; two per lane above 32; groups of <= 16 run
+                as several copies that split the source lists)
   lbits         tree depth, i.e. the depth of the walk (layers = lbits + 1)
   bucket        leaf tile size: an opened node holding <= bucket particles
                 is summed particle by particle
@@ -44,7 +44,7 @@ the CUDA-event time of graph-replayed steps (dt = 0, so every trial sees the
 same particles); the sort variant is judged by the sort stage's own time.
 
   python -m astro_gb300.autotune --workloads c1,c2,c3,c4,c5 --forms plain,precision \\
-      [--out astro_gb300/tuned.json]
+      [--lbits L] [--from-tuned] [--out astro_gb300/tuned.json]
 
 The result file holds, per "workload/form", the chosen knobs, the step time
 and error they gave, and every trial; bench.py reads it for its defaults.
@@ -80,7 +80,7 @@ def candidates(knob: str, n: int) -> list[int]:
     if knob == "bucket":
         return [8, 16, 32, 64]
     if knob == "group_size":
-        return [8, 12, 16, 24, 32]
+        return [8, 12, 16, 24, 32, 48, 64]
     if knob == "block_warps":
         return [4, 8]
     if knob == "sort_variant":
@@ -94,20 +94,30 @@ def candidates(knob: str, n: int) -> list[int]:
     raise KeyError(knob)
 
 
+def result_key(workload: str, form: str, lbits: int | None = None) -> str:
+    """Key of a result in the tuned file: "c2/plain", or "c5/plain@lbits6"
+    for a search at a fixed tree depth."""
+    return f"{workload}/{form}" + (f"@lbits{lbits}" if lbits is not None else "")
+
+
 def tune(workload: str, form: str, target: float = 1e-3, samples: int = 1024,
-         log=print) -> dict:
-    """Tune one workload with the library's native search (astro_autotune_ex)
-    from the preset's defaults at the workload's starting depth."""
+         lbits: int | None = None, start: dict | None = None, log=print) -> dict:
+    """Tune one workload with the library's native search
+    (astro_autotune_keep) from the preset's defaults (or the knobs `start`)
+    at the workload's starting depth, or holding the depth at `lbits`."""
     w = WORKLOADS[workload]
     pm, vr, sizes = w.make()
-    params = default_params(L.PRESET_PHYSICAL, form=FORMS[form], lbits=w.lbits, **w.physics)
+    knobs = dict(start or {})
+    knobs["lbits"] = lbits if lbits is not None else knobs.get("lbits", w.lbits)
+    params = default_params(L.PRESET_PHYSICAL, form=FORMS[form], **knobs, **w.physics)
     sim = Simulation(params, max_n=len(pm), max_systems=len(sizes) if sizes else 1)
     try:
         if sizes:
             sim.upload_systems(pm, vr, sizes)
         else:
             sim.upload(pm, vr)
-        res = sim.autotune(target=target, samples=samples)
+        res = sim.autotune(target=target, samples=samples,
+                           keep=L.TUNE_KEEP_LBITS if lbits is not None else 0)
     finally:
         sim.close()
     start = res["trials"][0]
@@ -137,14 +147,20 @@ def main(argv=None) -> int:
     ap.add_argument("--workloads", default="c1,c2,c3,c4,c5")
     ap.add_argument("--forms", default="plain,precision")
     ap.add_argument("--target", type=float, default=1e-3)
+    ap.add_argument("--lbits", type=int, default=None,
+                    help="hold the tree depth (result key workload/form@lbitsL)")
+    ap.add_argument("--from-tuned", action="store_true",
+                    help="start each search from the knobs already in the file")
     ap.add_argument("--out", type=Path, default=TUNED_PATH)
     args = ap.parse_args(argv)
     prev = json.loads(args.out.read_text()) if args.out.exists() else {"results": {}}
     results = prev.get("results", {})
     for wl in args.workloads.split(","):
         for form in args.forms.split(","):
-            r = tune(wl, form, args.target)
-            results[f"{wl}/{form}"] = r
+            key = result_key(wl, form, args.lbits)
+            start = results.get(key, {}).get("knobs") if args.from_tuned else None
+            r = tune(wl, form, args.target, lbits=args.lbits, start=start)
+            results[key] = r
             out = {"device": torch.cuda.get_device_name(),
                    "sms": torch.cuda.get_device_properties(0).multi_processor_count,
                    "when": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),

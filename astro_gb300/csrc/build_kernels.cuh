@@ -238,6 +238,9 @@ cudaError_t launch_traverse_phys(const TraverseArgs& a, const TraverseConfig& c,
 // then evaluation).
 uint32_t group_walk_warps();
 size_t group_list_blocks(uint32_t n, uint32_t group_size);
-cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);
+// ev (optional, three events): recorded before the walk, between the walk
+// and the evaluation, and after it.
+cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st,
+                                   cudaEvent_t* ev = nullptr);
 
 }  // namespace astro

@@ -411,7 +411,13 @@ int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
     if (group_walk(ctx)) {
         int r = ensure_frontier(ctx);
         if (r != ASTRO_OK) return r;
-        CK(astro::launch_traverse_groups(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
+        // Stage calls (outside stream capture) time the two kernels.
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(st, &cap));
+        const bool timed = cap == cudaStreamCaptureStatusNone;
+        CK(astro::launch_traverse_groups(traverse_args(ctx, dt, integrate), traverse_config(ctx), st,
+                                         timed ? ctx->trav_ev : nullptr));
+        ctx->trav_timed = timed;
     } else {
         CK(astro::launch_traverse_phys(traverse_args(ctx, dt, integrate), traverse_config(ctx), st));
     }
@@ -544,6 +550,9 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     ctx->p = *params;
     ctx->max_n = max_n;
     ctx->max_sys = max_systems;
+    // A walk frontier holds at most one layer's nodes of one system (node
+    // list) or one run per opened node (runs, two words each): 2 max_n words.
+    ctx->frontier_cap = (uint32_t)std::min<uint64_t>(16384, std::max<uint64_t>(64, 2ull * max_n));
     auto cleanup = [&](int code) {
         astro_destroy(ctx);
         return code;
@@ -580,6 +589,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     CKC(dev_alloc(&ctx->groups, max_n));
     CKC(dev_alloc(&ctx->err, 1));
     CKC(dev_alloc(&ctx->stats, kNumStats));
+    for (cudaEvent_t& e : ctx->trav_ev) CKC(cudaEventCreate(&e));
     CKC(dev_alloc(&ctx->layer_count, ASTRO_MAX_LAYERS));
     CKC(dev_alloc(&ctx->sys, max_systems));
     CKC(dev_alloc(&ctx->bbox32, 6ull * max_systems));
@@ -649,6 +659,8 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->list_next);
     dev_free(ctx->group_desc);
     if (ctx->readback) cudaFree(ctx->readback);
+    for (cudaEvent_t& e : ctx->trav_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return ASTRO_OK;
@@ -1001,6 +1013,18 @@ int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_inte
     if (far_nodes) *far_nodes = s[3];
     if (far_interactions) *far_interactions = s[4];
     return r;
+}
+
+int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!ctx->trav_timed) return fail(ctx, ASTRO_ERR_STATE, "no timed group walk stage call yet");
+    CK(cudaEventSynchronize(ctx->trav_ev[2]));
+    float w = 0.f, e = 0.f;
+    CK(cudaEventElapsedTime(&w, ctx->trav_ev[0], ctx->trav_ev[1]));
+    CK(cudaEventElapsedTime(&e, ctx->trav_ev[1], ctx->trav_ev[2]));
+    if (walk_ms) *walk_ms = w;
+    if (eval_ms) *eval_ms = e;
+    return ASTRO_OK;
 }
 
 int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t n_sample,

@@ -189,7 +189,7 @@ extern "C" int astro_generate_ic(uint32_t kind, uint64_t seed, uint32_t system, 
             for (uint32_t k = 0; k < n; ++k) menc[order[k]] = (k + 1) * m;
             for (uint32_t i = 0; i < n; ++i) {
                 Stream s(seed, system ^ 0x80000000u, i);
-                const double x = pm[i].position[0], y = pm[i].position[1], z = pm[i].position[2];
+                const double x = pm[i].position[0], y = pm[i].position[1];
                 const double rr = std::max(r[i], 1e-6);
                 if (i < nd) {
                     const double R = std::max(std::sqrt(x * x + y * y), 1e-6);

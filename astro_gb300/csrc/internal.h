@@ -139,7 +139,7 @@ struct astro_ctx {
     uint2* groups = nullptr;          // group-walk particle ranges (<= n)
     uint32_t* frontier = nullptr;     // group-walk per-warp frontier buffers
     size_t frontier_words = 0;
-    uint32_t frontier_cap = 16384;
+    uint32_t frontier_cap = 16384;   // words per frontier buffer (set by astro_create)
     astro::GroupDesc* group_desc = nullptr;  // group walk: per-group lists (<= max_n groups)
     uint32_t* lists = nullptr;        // group walk: list pool
     uint32_t* list_next = nullptr;    // group walk: block chain links
@@ -160,6 +160,9 @@ struct astro_ctx {
     size_t topo_lookback_words = 0;
     uint32_t* counters = nullptr;             // [0] topology tiles, [1] traversal queue, [2] groups
     uint32_t* err = nullptr;                  // device error word
+    cudaEvent_t trav_ev[3] = {nullptr, nullptr, nullptr};  // traversal stage call: before,
+                                              // between walk and evaluation, after
+    bool trav_timed = false;                  // the last traversal stage call recorded them
     unsigned long long* stats = nullptr;      // interactions, node visits, cell
                                               // interactions, far nodes, far interactions
     void* readback = nullptr;

@@ -89,7 +89,7 @@ struct ListTail {
 
 // Blocks of the pool a walk warp holds for its lists: [next, end), taken
 // from the pool kBlockBatch at a time (one atomic per batch).
-constexpr uint32_t kBlockBatch = 32;
+constexpr uint32_t kBlockBatch = 16;
 struct BlockCache {
     uint32_t next, end;
 };
@@ -997,24 +997,30 @@ size_t group_list_blocks(uint32_t n, uint32_t group_size) {
     // size. 2,048 words per group of half the group size, plus the batches of
     // blocks the walk warps hold, leaves room.
     const size_t groups = (size_t)n / std::max(1u, group_size / 2u) + 1;
-    const size_t words = std::max<size_t>(groups * 2048, (size_t)1 << 24);
+    const size_t words = std::max<size_t>(groups * 2048, (size_t)1 << 22);
     const size_t blocks = words / kListBlockWords + (size_t)group_walk_warps() * kBlockBatch;
     return std::min<size_t>(blocks, 0xFFFFFF00ull);
 }
 
-cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st) {
+cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st,
+                                   cudaEvent_t* ev) {
     if (a.n == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     // Evaluation queue and list pool counter (adjacent words).
     e = cudaMemsetAsync(a.eval_queue, 0, 2 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
+    if (ev && (e = cudaEventRecord(ev[0], st)) != cudaSuccess) return e;
     group_walk_kernel<<<walk_blocks(), kWalkWarps * 32, 0, st>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
     if (c.exact)
-        return c.precision ? launch_eval_q<true, true>(a, c, st) : launch_eval_q<true, false>(a, c, st);
-    return c.precision ? launch_eval_q<false, true>(a, c, st) : launch_eval_q<false, false>(a, c, st);
+        e = c.precision ? launch_eval_q<true, true>(a, c, st) : launch_eval_q<true, false>(a, c, st);
+    else
+        e = c.precision ? launch_eval_q<false, true>(a, c, st) : launch_eval_q<false, false>(a, c, st);
+    if (e != cudaSuccess) return e;
+    return ev ? cudaEventRecord(ev[2], st) : cudaSuccess;
 }
 
 }  // namespace astro

@@ -13,7 +13,8 @@
 // max(0.8 x target, 1.02 x the starting error); then lbits, bucket,
 // group_size, block_warps and walk_frontier once more within that bound. sort_variant is
 // judged by the sort stage's own time. theta, the softening, the walk flags
-// and the form are physics and stay as set.
+// and the form are physics and stay as set; astro_autotune_keep also holds
+// the knobs its caller names (a workload quoted at a given tree depth).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -44,8 +45,8 @@ enum Knob { kLbits, kBucket, kGroupSize, kBlockWarps, kSortVariant, kWalkFrontie
 
 class Tuner {
 public:
-    Tuner(astro_ctx* ctx, float target, uint32_t n_samples)
-        : ctx_(ctx), target_(target), n_samples_(n_samples) {}
+    Tuner(astro_ctx* ctx, float target, uint32_t n_samples, uint32_t keep)
+        : ctx_(ctx), target_(target), n_samples_(n_samples), keep_(keep) {}
     ~Tuner() {
         for (cudaEvent_t& e : ev_)
             if (e) cudaEventDestroy(e);
@@ -62,6 +63,7 @@ private:
     astro_ctx* ctx_;
     float target_;
     uint32_t n_samples_;
+    uint32_t keep_;  // ASTRO_TUNE_KEEP_* knobs held at the starting values
     astro_params base_{};
     std::vector<PositionMass> pm_;
     std::vector<VelocityRadius> vr_;
@@ -188,7 +190,7 @@ std::vector<uint32_t> Tuner::candidates(Knob knob) const {
             return c;
         }
         case kBucket: return {8, 16, 32, 64};
-        case kGroupSize: return {8, 12, 16, 24, 32};
+        case kGroupSize: return {8, 12, 16, 24, 32, 48, 64};
         case kBlockWarps: return {4, 8};
         case kSortVariant: return {1, 2, 3, 4, 5, 6, 7, 8, 9};
         case kWalkFrontier: return {0, 1};
@@ -197,6 +199,9 @@ std::vector<uint32_t> Tuner::candidates(Knob knob) const {
 }
 
 int Tuner::sweep(Knob knob, double limit, Trial* best) {
+    if ((knob == kLbits && (keep_ & ASTRO_TUNE_KEEP_LBITS)) ||
+        (knob == kGroupSize && (keep_ & ASTRO_TUNE_KEEP_GROUP_SIZE)))
+        return ASTRO_OK;
     for (uint32_t v : candidates(knob)) {
         Knobs k = best->k;
         uint32_t* field = knob == kLbits ? &k.lbits : knob == kBucket ? &k.bucket
@@ -289,6 +294,7 @@ int Tuner::run(const char* path) {
     // The accuracy knobs share one error budget.
     const Knobs base = best.k;
     for (float w : {1.0f, 0.85f, 0.7f, 0.5f}) {
+        if (keep_ & ASTRO_TUNE_KEEP_ACCURACY) break;
         for (float f : {0.0f, 0.1f, 0.15f, 0.2f, 0.25f, 0.3f, 0.4f, 0.5f}) {
             Knobs k = base;
             k.open_delta_weight = w;
@@ -310,8 +316,13 @@ int Tuner::run(const char* path) {
 
 }  // namespace
 
-extern "C" int astro_autotune_ex(astro_ctx* ctx, const char* path, float target, uint32_t samples) {
+extern "C" int astro_autotune_keep(astro_ctx* ctx, const char* path, float target, uint32_t samples,
+                                   uint32_t keep) {
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (keep & ~(ASTRO_TUNE_KEEP_LBITS | ASTRO_TUNE_KEEP_GROUP_SIZE | ASTRO_TUNE_KEEP_ACCURACY)) {
+        ctx->last_error = "autotune: unknown ASTRO_TUNE_KEEP_* bits";
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    }
     if (!ctx->uploaded) {
         ctx->last_error = "autotune: no particles uploaded";
         return ASTRO_ERR_STATE;
@@ -324,7 +335,7 @@ extern "C" int astro_autotune_ex(astro_ctx* ctx, const char* path, float target,
         ctx->last_error = "autotune: target must be > 0 and samples > 0";
         return ASTRO_ERR_INVALID_ARGUMENT;
     }
-    Tuner t(ctx, target, samples);
+    Tuner t(ctx, target, samples, keep);
     const astro_params before = ctx->p;
     const int r = t.run(path);
     if (r != ASTRO_OK) {
@@ -333,6 +344,10 @@ extern "C" int astro_autotune_ex(astro_ctx* ctx, const char* path, float target,
         ctx->last_error = why;
     }
     return r;
+}
+
+extern "C" int astro_autotune_ex(astro_ctx* ctx, const char* path, float target, uint32_t samples) {
+    return astro_autotune_keep(ctx, path, target, samples, 0u);
 }
 
 extern "C" int astro_autotune(astro_ctx* ctx, const char* path) {

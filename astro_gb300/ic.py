@@ -13,12 +13,38 @@ import numpy as np
 from . import layouts as L
 from ._native import check, lib, ptr
 
+# The library whose astro_generate_ic / astro_generate_system_sizes make the
+# particles: libastro_cuda unless a caller names another build of the same
+# host source (ic.cpp) with use_generator_library().
+_generator = None
+
+
+def use_generator_library(cdll) -> None:
+    """Generate with `cdll` (a ctypes library exporting astro_generate_ic and
+    astro_generate_system_sizes from the same source); None restores the
+    default."""
+    global _generator
+    if cdll is not None:
+        from ctypes import c_double, c_int, c_uint32, c_uint64
+
+        cdll.astro_generate_ic.restype = c_int
+        cdll.astro_generate_ic.argtypes = [c_uint32, c_uint64, c_uint32, c_uint32, c_double,
+                                           c_double, c_void_p, c_void_p, c_void_p]
+        cdll.astro_generate_system_sizes.restype = c_int
+        cdll.astro_generate_system_sizes.argtypes = [c_uint64, c_uint32, c_uint32, c_uint32,
+                                                     c_double, c_double, c_void_p, c_void_p]
+    _generator = cdll
+
+
+def _gen():
+    return _generator if _generator is not None else lib()
+
 
 def generate(kind: int, n: int, seed: int, system: int = 0, p0: float = 0.0, p1: float = 0.0,
              with_colors: bool = False):
     pm, vr = L.empty_particles(n)
     ct = np.zeros(n, L.COLOR_TYPE) if with_colors else None
-    check(lib().astro_generate_ic(kind, seed, system, n, p0, p1, ptr(pm), ptr(vr),
+    check(_gen().astro_generate_ic(kind, seed, system, n, p0, p1, ptr(pm), ptr(vr),
                                   ptr(ct) if ct is not None else c_void_p(0)))
     return (pm, vr, ct) if with_colors else (pm, vr)
 
@@ -50,7 +76,7 @@ def system_sizes(nsys: int, seed: int, n_min: int = 1024, n_max: int = 65536,
                  a_min: float = 0.5, a_max: float = 2.0):
     sizes = np.zeros(nsys, np.uint32)
     scales = np.zeros(nsys, np.float64)
-    check(lib().astro_generate_system_sizes(seed, nsys, n_min, n_max, a_min, a_max, ptr(sizes),
+    check(_gen().astro_generate_system_sizes(seed, nsys, n_min, n_max, a_min, a_max, ptr(sizes),
                                             ptr(scales)))
     return sizes, scales
 

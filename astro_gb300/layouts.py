@@ -25,6 +25,10 @@ FLAG_PERSISTENT = 0x4
 FLAG_OPEN_DELTA = 0x8
 FLAG_QUADRUPOLE = 0x10
 FLAG_PER_PARTICLE = 0x20
+# astro_autotune_keep: knobs held at the context's values.
+TUNE_KEEP_LBITS = 0x1
+TUNE_KEEP_GROUP_SIZE = 0x2
+TUNE_KEEP_ACCURACY = 0x4
 
 IC_PLUMMER = 0
 IC_DISK_BULGE = 1
@@ -94,6 +98,37 @@ class Params(ctypes.Structure):
         d = {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("_")}
         d["type_accel_scale"] = list(self.type_accel_scale)
         return d
+
+
+def host_default_params(preset: int = PRESET_PHYSICAL, **overrides) -> Params:
+    """astro_params_default restated on the host (no library load): for
+    callers that only hand parameters to a CPU implementation. A CPU test
+    checks that both give the same bytes."""
+    p = Params()
+    p.preset = preset
+    p.form = FORM_PLAIN
+    p.lbits = 6                 # MortonCode.metal:47-50
+    p.theta = 0.7               # Renderer.swift:864
+    p.open_delta_weight = 1.0
+    p.force_clamp = 1e5         # BarnesHut.metal:100
+    if preset == PRESET_REFERENCE:
+        p.g = 1e11              # BarnesHut.metal:39
+        p.softening = 0.01      # BarnesHut.metal:40
+        p.leaf_min_dist2 = 50.0  # BarnesHut.metal:70
+        p.quant_offset = 1e6    # MortonCode.metal:35-37
+        p.damping = 0.9995      # BarnesHut.metal:189
+        p.type_accel_scale = (ctypes.c_float * 3)(5.0, 5.0, 1.0)  # BarnesHut.metal:181-187
+        p.light_sources = 5     # numStars (Renderer.swift:26)
+    elif preset == PRESET_PHYSICAL:
+        p.g = 1.0
+        p.softening = 0.01
+        p.damping = 1.0
+        p.type_accel_scale = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+        p.bucket = 16
+        p.flags = FLAG_OPEN_DELTA | FLAG_QUADRUPOLE
+    else:
+        raise ValueError(f"unknown preset {preset}")
+    return p.replace(**overrides) if overrides else p
 
 
 def empty_particles(n: int):

@@ -164,10 +164,11 @@ class Simulation:
         sz = np.ascontiguousarray(sizes, dtype=np.uint32)
         self._check(lib().astro_step_batched(self._h, ptr(sz), len(sz), dt, steps))
 
-    def autotune(self, path=None, target: float = 1e-3, samples: int = 1024) -> dict:
-        """Native autotuner (astro_autotune_ex) on the current particles: the
-        best knobs are applied to this context; returns the result record
-        (knobs, step time, error, trials)."""
+    def autotune(self, path=None, target: float = 1e-3, samples: int = 1024, keep: int = 0) -> dict:
+        """Native autotuner (astro_autotune_keep) on the current particles,
+        holding the knobs of `keep` (TUNE_KEEP_* bits): the best knobs are
+        applied to this context; returns the result record (knobs, step
+        time, error, trials)."""
         import json
         import os
         import tempfile
@@ -178,7 +179,7 @@ class Simulation:
             os.close(fd)
             path = tmp
         try:
-            self._check(lib().astro_autotune_ex(self._h, str(path).encode(), target, samples))
+            self._check(lib().astro_autotune_keep(self._h, str(path).encode(), target, samples, keep))
             with open(path) as f:
                 out = json.load(f)
         finally:
@@ -241,6 +242,12 @@ class Simulation:
         f, fi = c_uint64(), c_uint64()
         self._check(lib().astro_read_far_stats(self._h, byref(f), byref(fi)))
         return f.value, fi.value
+
+    def traverse_times(self) -> tuple[float, float]:
+        """(walk ms, evaluation ms) of the last group-walk barnes_hut() call."""
+        w, e = ctypes.c_float(), ctypes.c_float()
+        self._check(lib().astro_read_traverse_times(self._h, byref(w), byref(e)))
+        return w.value, e.value
 
     def direct_accel_f64(self, samples) -> np.ndarray:
         s = np.ascontiguousarray(samples, dtype=np.uint32)

@@ -5,7 +5,8 @@ c1  Plummer sphere a=1, N=16,384
 c2  exponential disk (R_d=1, z_d=0.1, 80% of the mass) + Hernquist bulge, N=524,288
 c3  two Plummer spheres a=1, M=0.5 each, separation 10, N=4,194,304
 c4  256 Plummer systems, N_s log-uniform in [1024, 65536] (batched)
-c5  uniform unit cube, log-normal masses, N=16,777,216
+c5  uniform unit cube, log-normal masses, N=16,777,216, quoted at the
+    reference's 7 layers (lbits 6) and at all 21 bits (lbits 21)
 ref the reference's own scene (Renderer.swift:25-46,441-493): 5 stars and 200
     planets in the tree, 500,000 dust tracers, REFERENCE preset
 
@@ -27,8 +28,9 @@ class Workload:
     seed: int
     dt: float
     physics: dict = field(default_factory=dict)   # astro_params overrides (softening, ...)
-    lbits: int = 14       # tree depth the workload is quoted at before tuning
+    lbits: int = 14       # tree depth the autotuner starts from
     preset: str = "physical"
+    quoted_lbits: int | None = None  # tree depth the workload is quoted at (held fixed)
 
     def make_colors(self):
         """ColorType[] and the tree count of the REFERENCE scene."""
@@ -61,7 +63,7 @@ WORKLOADS = {
     "c4": Workload("c4", "256 Plummer systems, N_s log-uniform [1024, 65536]", "batch", 0, 1004,
                    1e-3, dict(softening=0.01)),
     "c5": Workload("c5", "uniform unit cube, log-normal masses, N=16777216", "uniform_cube",
-                   16777216, 1005, 1e-3, dict(softening=0.001)),
+                   16777216, 1005, 1e-3, dict(softening=0.001), quoted_lbits=6),
     "ref": Workload("ref", "the reference's scene: 5 stars + 200 planets in the tree, 500,000 dust "
                     "tracers (REFERENCE preset)", "reference_scene", 500205, 1, 1.0 / 60.0, {}, 6,
                     "reference"),

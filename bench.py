@@ -1,26 +1,34 @@
 """Benchmark of the Barnes-Hut step on GB300: particle-updates/s.
 
-Default workload (the configuration the metric is quoted on): a seeded
-rotating exponential disk (R_d = 1, z_d = 0.1, 80% of the mass) plus a
-Hernquist bulge (20%), N = 524,288, PHYSICAL preset, plain FP32, theta = 0.7,
-eps = 0.005, dt = 5e-4. One step = bbox, encode, sort, Morton reorder, tree
-topology, per-layer aggregation, traversal with the fused kick-drift.
+Default workload (the largest configuration on one GPU, at the tree depth the
+reference uses): N = 16,777,216 particles uniform in a unit cube (seeded
+Gaussian velocities, sigma 0.1; log-normal masses, sigma 0.5, total 1),
+PHYSICAL preset, plain FP32, theta = 0.7, eps = 0.001, dt = 1e-3, lbits = 6
+(the reference's 7 layers, MortonCode.metal:43-50). One step = bbox,
+encode, sort, Morton reorder, tree topology, per-layer aggregation, the
+group walk and its evaluation with the fused kick-drift.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c1|c2|c3|c4|c5] [--form plain|precision]
+                  [--workload c1|c2|c3|c4|c5|ref] [--form plain|precision]
 
 `value` is the device-timed throughput with inputs resident in HBM (CUDA
 events on the context's stream around each step, L2 flushed before every
 timed step). `e2e` is the same metric through the C ABI with host buffers:
 each step uploads PositionMass/VelocityRadius from pinned host memory, steps
-and downloads them. `--impl reference` times the CPU restatement of the
-reference kernels (oracle/, OpenMP over all host cores) on the same workload.
-Under torchrun every rank runs an independent replica (the single-system step
-does not shard); rank 0 prints the line with the max time over ranks.
+and downloads them. Extra keys of the default line: the same workload with
+all 21 bits per axis (63-bit keys) and in the precision form, and the
+metric's comparison on the batching workload (256 Plummer systems): plain
+FP32 batched, precision + batched, and the systems stepped one at a time.
+`--impl reference` times the CPU restatement of the reference kernels
+(oracle/, OpenMP over all host cores) on the same workload within a time
+budget. Under torchrun every rank runs an independent replica (the
+single-system step does not shard); rank 0 prints the line with the max
+time over ranks.
 """
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import datetime
 import json
 import os
@@ -51,24 +59,26 @@ FLOPS_PER_QUAD_CELL = 50
 FLOPS_PER_FAR_NODE = 350
 FLOPS_PER_FAR_EVAL = 70
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one traversal
-# launch, captured with ncu on GB300 for (workload, form, walk) at the tuned
-# knobs: the roofline's "traffic".
-NCU_TRAVERSAL_DRAM_BYTES = {("c2", "plain", "group"): 51.2e6}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the group evaluation kernel, from one ncu capture on GB300 for (workload,
+# form, lbits) at the tuned knobs: the roofline's "traffic".
+NCU_EVAL_DRAM_BYTES: dict = {}
 
-def parse():
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2",
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c5",
                     help="c1..c5: PHYSICAL workloads; ref: the reference's own scene")
     ap.add_argument("--form", choices=["plain", "precision"], default="plain")
     ap.add_argument("--n", type=int, default=None,
                     help="particles of a single-system workload (smaller cases for profiling)")
     # Launch knobs: unset ones come from the autotuner's file for the
-    # workload and form (astro_gb300/tuned.json), else the preset defaults.
+    # workload, form and tree depth (astro_gb300/tuned.json), else the
+    # preset defaults. The tree depth defaults to the workload's quoted one.
     ap.add_argument("--lbits", type=int, default=None)
     ap.add_argument("--bucket", type=int, default=None)
     ap.add_argument("--warps", type=int, default=None)
@@ -91,40 +101,42 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-threads", type=int, default=0,
                     help="host threads of the CPU restatement (0: all cores)")
+    ap.add_argument("--reference-seconds", type=float, default=120.0,
+                    help="--impl reference: time budget of the timed CPU steps")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--one-at-a-time", action="store_true",
-                    help="batched workload: also time the systems stepped one at a time")
-    return ap.parse_args()
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the extra configurations of the default line")
+    return ap.parse_args(argv)
 
 
 def workload(args):
     """The workload of --workload, with --n particles when given."""
-    import dataclasses
-
     w = WORKLOADS[args.workload]
-    if args.n is not None:
+    n = getattr(args, "n", None)
+    if n is not None:
         if w.generator in ("batch", "reference_scene"):
             raise SystemExit("--n applies to the single-system PHYSICAL workloads")
-        w = dataclasses.replace(w, n=args.n)
+        w = dataclasses.replace(w, n=n)
     return w
 
 
 CLIMB_MIN_NODES = 32768  # build.cu: layers of at least this capacity get a launch each
 
 
-def kernels_per_step(key_bits: int, layer_sizes) -> int:
+def kernels_per_step(key_bits: int, layer_sizes, preset: str = "physical") -> int:
     """This library's kernel launches in one step. PHYSICAL: bbox, setup,
     encode, sort histogram + one pass per 8 key bits, Morton reorder,
     topology, the per-layer aggregations below the climb + the climbing
-    one, traversal. REFERENCE: encode, sort histogram + passes, topology,
-    aggregations, traversal, lights snapshot + lighting, integrate. Both
-    come to 8 + passes + the per-layer aggregation launches."""
+    one, the group walk and its evaluation (9 + passes + per-layer
+    aggregations). REFERENCE: encode, sort histogram + passes, topology,
+    aggregations, traversal, lights snapshot + lighting, integrate (8 +
+    passes + per-layer aggregations)."""
     passes = (key_bits + 7) // 8
     l0 = 0
     while l0 + 1 < len(layer_sizes) and layer_sizes[l0] >= CLIMB_MIN_NODES:
         l0 += 1
-    return 8 + passes + l0
+    return (9 if preset == "physical" else 8) + passes + l0
 
 
 def walk_flags(args, L, flags):
@@ -138,13 +150,29 @@ def walk_flags(args, L, flags):
     return flags
 
 
+def quoted_lbits(args):
+    """The tree depth the line is quoted at: --lbits, else the workload's
+    quoted depth (c5: the reference's 7 layers), else None (tuned)."""
+    if args.lbits is not None:
+        return args.lbits, "command line"
+    w = WORKLOADS[args.workload]
+    if w.quoted_lbits is not None:
+        return w.quoted_lbits, "the workload's quoted depth"
+    return None, None
+
+
 def knobs(args):
-    """Launch knobs: command line, else the tuned file, else the defaults."""
+    """Launch knobs: command line, else the tuned file (the entry searched at
+    the quoted tree depth when there is one), else the defaults."""
     tuned = {}
+    lbits, lsrc = quoted_lbits(args)
     if not args.no_tuned:
         from astro_gb300 import autotune
 
-        tuned = autotune.load().get(f"{args.workload}/{args.form}", {}).get("knobs", {})
+        res = autotune.load()
+        key = autotune.result_key(args.workload, args.form, lbits)
+        entry = res.get(key) or res.get(autotune.result_key(args.workload, args.form))
+        tuned = (entry or {}).get("knobs", {})
     default = {"lbits": WORKLOADS[args.workload].lbits, "bucket": 16, "block_warps": 0,
                "group_size": 0, "sort_variant": 0, "open_delta_weight": 1.0, "far_ratio": 0.0,
                "walk_frontier": 0}
@@ -156,6 +184,8 @@ def knobs(args):
     for k in default:
         if given[k] is not None:
             out[k], source[k] = given[k], "command line"
+        elif k == "lbits" and lbits is not None:
+            out[k], source[k] = lbits, lsrc
         elif k in tuned:
             out[k], source[k] = tuned[k], "autotuner"
         else:
@@ -163,7 +193,7 @@ def knobs(args):
     return out, source
 
 
-def make_params(args, ag, L):
+def make_params(args, L, default_params):
     w = workload(args)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     k, source = knobs(args)
@@ -172,8 +202,8 @@ def make_params(args, ag, L):
         # apply to its walk.
         k = {key: k[key] for key in ("lbits", "sort_variant")}
         source = {key: source[key] for key in k}
-        return ag.default_params(L.PRESET_REFERENCE, theta=args.theta, **k), source
-    p = ag.default_params(L.PRESET_PHYSICAL, theta=args.theta, form=form, **k, **w.physics)
+        return default_params(L.PRESET_REFERENCE, theta=args.theta, **k), source
+    p = default_params(L.PRESET_PHYSICAL, theta=args.theta, form=form, **k, **w.physics)
     return p.replace(flags=walk_flags(args, L, p.flags)), source
 
 
@@ -330,12 +360,46 @@ def sort_alone(torch, n, key_bits, seed, flush, stream, sim, peaks):
         sim.synchronize()
         if it:
             sort_ms.append(e0.elapsed_time(e1))
+    sorter.status(sim.stream)
     passes = (key_bits + 7) // 8
     sort_b = (8 + 24 * passes - 4) * n
     ms = float(np.mean(sort_ms))
     return {"bound": "hbm", "key_bits": key_bits, "passes": passes, "keys": n, "bytes": sort_b,
             "ms": ms, "achieved": sort_b / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": sort_b / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+
+
+def error_vs_direct(sim, n, seed, samples):
+    """Median and p99 relative acceleration error against the FP64 direct
+    sum on sampled particles (current state; forces only, the state is kept)."""
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(n, size=min(samples, n), replace=False)).astype(np.uint32)
+    sim.generate_morton_codes()
+    sim.sort()
+    sim.build_tree()
+    sim.barnes_hut()
+    acc = sim.read_accel()
+    direct = sim.direct_accel_f64(idx)
+    sim.update_spheres(0.0)
+    err = np.linalg.norm(acc[idx, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    return {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
+            "samples": int(len(err))}
+
+
+def timed_steps(torch, sim, dt, steps, flush, stream):
+    """K steps, each after an L2 flush, timed by CUDA events on the
+    context's stream; returns the per-step milliseconds."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+            sim.draw(dt, 1)
+            ends[k].record(stream)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
 
 # ---------------------------------------------------------------- ours --
@@ -352,7 +416,7 @@ def run_ours(args, world, rank, local):
     pm, vr, sizes = w.make()
     n = len(pm)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
-    p, knob_source = make_params(args, ag, L)
+    p, knob_source = make_params(args, L, ag.default_params)
     nsys = len(sizes) if sizes else 1
     is_ref = w.preset == "reference"
     ct, n_tree = w.make_colors() if is_ref else (None, n)
@@ -375,30 +439,20 @@ def run_ours(args, world, rank, local):
 
     # Timed region: K steps, each after an L2 flush, timed by CUDA events on
     # the context's stream.
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         clk.mark_start()
         t0 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                flush.fill_(k & 0xFF)
-                starts[k].record(stream)
-                sim.draw(dt, 1)
-                ends[k].record(stream)
-        sim.synchronize()
-        torch.cuda.synchronize()
+        step_ms = timed_steps(torch, sim, dt, args.steps, flush, stream)
         wall = time.perf_counter() - t0
         clk.mark_end()
     barrier(world)
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = sum(step_ms)
     t_ms_max = reduce_max(t_ms, world)
     value = n * args.steps * world / (t_ms_max * 1e-3)
 
-    # One instrumented step: per-stage times and the traversal's roofline.
+    # One instrumented step: per-stage times.
     stages = {}
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     with torch.cuda.stream(stream):
@@ -436,14 +490,17 @@ def run_ours(args, world, rank, local):
     if not is_ref:
         sort_roofline = sort_alone(torch, n, key_bits, w.seed, flush, stream, sim, peaks)
     quad = (p.flags & L.FLAG_QUADRUPOLE) != 0
+    group = not is_ref and args.walk == "group"
 
     far_nodes, far_inter = sim.read_far_stats() if not is_ref else (0, 0)
     flops = (FLOPS_PER_QUAD_CELL if quad else FLOPS_PER_INTERACTION) * (cell_inter - far_inter) + \
         FLOPS_PER_INTERACTION * (interactions - cell_inter) + FLOPS_PER_FAR_NODE * far_nodes + \
         (FLOPS_PER_FAR_EVAL * n if far_nodes else 0)
 
-    # Traversal alone, several launches after a flush each, for the roofline.
-    trav_ms = []
+    # Traversal alone, several launches after a flush each, for the roofline:
+    # the group walk's two kernels timed apart (events recorded by the
+    # library between them), the other walks as one kernel.
+    trav_ms, walk_ms, eval_ms = [], [], []
     for _ in range(3):
         with torch.cuda.stream(stream):
             sim.generate_morton_codes()
@@ -457,26 +514,18 @@ def run_ours(args, world, rank, local):
             sim.update_spheres(0.0)
         sim.synchronize()
         trav_ms.append(e0.elapsed_time(e1))
+        if group:
+            wm, em = sim.traverse_times()
+            walk_ms.append(wm)
+            eval_ms.append(em)
     trav = float(np.mean(trav_ms))
+    kernel_ms = float(np.mean(eval_ms)) if group else trav
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     fp32_peak = 2 * 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    achieved = flops / (trav * 1e-3) / 1e12
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
 
-    # Error against the FP64 direct sum on sampled particles (current state;
-    # PHYSICAL units only).
-    err = None
-    if not is_ref:
-        rng = np.random.default_rng(w.seed)
-        samples = np.sort(rng.choice(n, size=min(args.error_samples, n), replace=False)).astype(
-            np.uint32)
-        sim.generate_morton_codes()
-        sim.sort()
-        sim.build_tree()
-        sim.barnes_hut()
-        acc = sim.read_accel()
-        direct = sim.direct_accel_f64(samples)
-        sim.update_spheres(0.0)
-        err = np.linalg.norm(acc[samples, :3] - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    # Error against the FP64 direct sum on sampled particles (PHYSICAL units only).
+    err = None if is_ref else error_vs_direct(sim, n, w.seed, args.error_samples)
 
     # End to end through the C ABI with pinned host buffers.
     e2e = None
@@ -487,16 +536,14 @@ def run_ours(args, world, rank, local):
         hvr = pin_vr.numpy().view(L.VELOCITY_RADIUS)
         hpm[:] = pm
         hvr[:] = vr
-        def up():
-            upload_from(hpm, hvr)
         for _ in range(max(1, args.warmup)):
-            up()
+            upload_from(hpm, hvr)
             sim.draw(dt, 1)
             sim.download(hpm, hvr)
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            up()
+            upload_from(hpm, hvr)
             sim.draw(dt, 1)
             sim.download(hpm, hvr)
         te = time.perf_counter() - t0
@@ -505,57 +552,127 @@ def run_ours(args, world, rank, local):
                "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 64 * n,
                "ms_per_step": te * 1e3 / args.steps}
 
-    # Batched workload: the same systems launched one at a time (one context
-    # and one step graph per system, stepped in sequence).
-    one_at_a_time = None
-    if sizes and args.one_at_a_time:
-        sims, off = [], 0
-        p_plain = p.replace(form=L.FORM_PLAIN)
+    launches_per_step = kernels_per_step(key_bits, sizes_, w.preset)
+    sim.close()
+    del flush
+    torch.cuda.empty_cache()
+    return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
+                wall=wall, step_ms=step_ms, stages=stages, interactions=interactions,
+                visits=visits, cell_inter=cell_inter, flops=flops, far_nodes=far_nodes,
+                far_inter=far_inter, counts=[int(c) for c in counts], trav_ms=trav,
+                kernel_ms=kernel_ms, walk_ms=float(np.mean(walk_ms)) if walk_ms else None,
+                achieved=achieved, fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e,
+                clocks=clk.summary(), launches=launches_per_step * args.steps, sizes=sizes, pm=pm,
+                vr=vr, stage_roofline=stage_roofline, sort_roofline=sort_roofline)
+
+
+def run_variant(torch, args, workload_name, form, lbits, steps, warmup, error_samples=512):
+    """Another configuration of the line: workload `workload_name` in `form`
+    at tree depth `lbits` (None: tuned), its tuned knobs, `steps` timed
+    steps after an L2 flush each. Returns its throughput, step time, knobs
+    and error (PHYSICAL workloads)."""
+    import astro_gb300 as ag
+    from astro_gb300 import layouts as L
+
+    va = argparse.Namespace(**{**vars(args), "workload": workload_name, "form": form,
+                               "lbits": lbits, "n": None, "bucket": None, "warps": None,
+                               "group_size": None, "sort_variant": None, "delta_weight": None,
+                               "far_ratio": None, "walk_frontier": None})
+    w = WORKLOADS[workload_name]
+    pm, vr, sizes = w.make()
+    n = len(pm)
+    p, source = make_params(va, L, ag.default_params)
+    sim = ag.Simulation(p, max_n=n, max_systems=len(sizes) if sizes else 1)
+    try:
+        if sizes:
+            sim.upload_systems(pm, vr, sizes)
+        else:
+            sim.upload(pm, vr)
+        stream = torch.cuda.ExternalStream(sim.stream)
+        flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            sim.draw(w.dt, 1)
+        sim.synchronize()
+        ms = timed_steps(torch, sim, w.dt, steps, flush, stream)
+        err = error_vs_direct(sim, n, w.seed, error_samples)
+        k, _ = knobs(va)
+        return {"workload": f"{workload_name}: {w.description}", "form": form, "lbits": p.lbits,
+                "value": n * steps / (sum(ms) * 1e-3), "unit": UNIT,
+                "ms_per_step": float(np.mean(ms)), "steps": steps, "knobs": k,
+                "knob_source": source, "error_vs_fp64_direct": err}
+    finally:
+        sim.close()
+        torch.cuda.empty_cache()
+
+
+def one_at_a_time(torch, args, steps, warmup):
+    """The batching workload's systems stepped one at a time in plain FP32:
+    one context and step graph per system, each system's step launched
+    after the previous one finished (an event chain across the contexts'
+    streams, no host synchronisation)."""
+    import astro_gb300 as ag
+    from astro_gb300 import layouts as L
+
+    w = WORKLOADS["c4"]
+    pm, vr, sizes = w.make()
+    va = argparse.Namespace(**{**vars(args), "workload": "c4", "form": "plain", "lbits": None,
+                               "n": None})
+    p, _ = make_params(va, L, ag.default_params)
+    sims, off = [], 0
+    try:
         for sz in sizes:
-            s1 = ag.Simulation(p_plain, max_n=sz)
+            s1 = ag.Simulation(p, max_n=sz)
             s1.upload(pm[off:off + sz], vr[off:off + sz])
             off += sz
-            s1.draw(dt, 2)
+            s1.draw(w.dt, max(1, warmup))
             sims.append(s1)
         for s1 in sims:
             s1.synchronize()
-        # Each system's step waits for the previous one (an event chain
-        # across the contexts' streams), so the systems run one at a time on
-        # the device, as separate launches, without host synchronisation.
         streams = [torch.cuda.ExternalStream(s1.stream) for s1 in sims]
         torch.cuda.synchronize()
-        k1 = max(1, args.steps // 4)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(streams[0])
         prev = e0
-        for _ in range(k1):
+        for _ in range(steps):
             for s1, st1 in zip(sims, streams):
                 st1.wait_event(prev)
-                s1.draw(dt, 1)
+                s1.draw(w.dt, 1)
                 prev = torch.cuda.Event()
                 prev.record(st1)
         streams[0].wait_event(prev)
         e1.record(streams[0])
         torch.cuda.synchronize()
         t1 = e0.elapsed_time(e1)
-        one_at_a_time = {"value": n * k1 / (t1 * 1e-3), "unit": UNIT, "steps": k1,
-                         "ms_per_step": t1 / k1,
-                         "how": "plain FP32, one context and step graph per system, "
-                                "each system's step waiting for the previous one"}
+        return {"value": len(pm) * steps / (t1 * 1e-3), "unit": UNIT, "steps": steps,
+                "ms_per_step": t1 / steps, "form": "plain",
+                "how": "plain FP32, one context and step graph per system, each system's step "
+                       "waiting for the previous one"}
+    finally:
         for s1 in sims:
             s1.close()
+        torch.cuda.empty_cache()
 
-    launches_per_step = kernels_per_step(key_bits, sizes_)
-    sim.close()
-    return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
-                wall=wall,
-                step_ms=step_ms, stages=stages, interactions=interactions, visits=visits,
-                cell_inter=cell_inter, flops=flops, far_nodes=far_nodes, far_inter=far_inter,
-                counts=[int(c) for c in counts], trav_ms=trav, achieved=achieved,
-                fp32_peak=fp32_peak, peak_src=peak_src, err=err, e2e=e2e, clocks=clk.summary(),
-                launches=launches_per_step * args.steps, sizes=sizes, pm=pm, vr=vr,
-                one_at_a_time=one_at_a_time, stage_roofline=stage_roofline,
-                sort_roofline=sort_roofline)
+
+def extras(args):
+    """The default line's other configurations: C5 at lbits 21 (63-bit keys)
+    and in the precision form, and the batching workload plain batched,
+    precision + batched and one system at a time."""
+    import torch
+
+    k = max(3, args.steps // 4)
+    out = {}
+    if args.workload == "c5" and args.form == "plain":
+        out["c5_lbits21"] = run_variant(torch, args, "c5", "plain", 21, k, args.warmup)
+        out["c5_precision"] = run_variant(torch, args, "c5", "precision", 6, k, args.warmup)
+    plain = run_variant(torch, args, "c4", "plain", None, k, args.warmup)
+    prec = run_variant(torch, args, "c4", "precision", None, k, args.warmup)
+    alone = one_at_a_time(torch, args, max(2, k // 2), args.warmup)
+    out["batching"] = {
+        "workload": plain["workload"], "plain_batched": plain, "precision_batched": prec,
+        "plain_one_at_a_time": alone,
+        "precision_batched_over_plain_batched": prec["value"] / plain["value"],
+        "precision_batched_over_one_at_a_time": prec["value"] / alone["value"]}
+    return out
 
 
 # ----------------------------------------------------------- CPU side --
@@ -592,30 +709,40 @@ def cpu_run(args, pm, vr, sizes, p, dt, budget_s):
 
 
 def run_reference(args):
-    """--impl reference: the CPU restatement timed on the host cores."""
-    import astro_gb300 as ag
+    """--impl reference: the CPU restatement timed on the host cores. Inputs
+    and parameters are made without loading the CUDA library (the
+    generators come from the oracle's build of the same host source)."""
+    from astro_gb300 import ic
     from astro_gb300 import layouts as L
     from oracle import oracle as orc
 
+    ic.use_generator_library(orc.lib())
     w = workload(args)
     desc, dt = w.description, w.dt
     pm, vr, sizes = w.make()
     n = len(pm)
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
-    p, knob_source = make_params(args, ag, L)
+    p, knob_source = make_params(args, L, L.host_default_params)
     cores = orc.set_threads(args.cpu_threads)
     pm_c, vr_c = pm.copy(), vr.copy()
-    for _ in range(args.warmup):
+    # Warm-up: at most one step (a CPU step warms nothing up beyond the first).
+    for _ in range(min(args.warmup, 1)):
         cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    # Timed: up to K whole steps, stopping once the time budget is spent.
+    steps, t = 0, 0.0
+    while steps < max(1, args.steps):
+        t0 = time.perf_counter()
         cpu_step(orc, w, p, pm_c, vr_c, sizes, dt)
-    t = time.perf_counter() - t0
-    value = n * args.steps / t
-    sample = f"{args.steps} whole steps of the workload (N={n}), 64 one-bit split passes per sort"
+        t += time.perf_counter() - t0
+        steps += 1
+        if t >= args.reference_seconds:
+            break
+    value = n * steps / t
+    sample = (f"{steps} whole step(s) of the workload (N={n}) of the {args.steps} asked, within a "
+              f"{args.reference_seconds:g} s budget; 64 one-bit split passes per sort")
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": steps,
+        "warmup": min(args.warmup, 1), "ms_per_step": t * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if form == 0 else "f32+f64",
         "data": "synthetic (seeded, Philox4x32-10)", "impl": "reference",
         "config": config_dict(args, desc, n, dt, p, knob_source),
@@ -634,7 +761,8 @@ def config_dict(args, desc, n, dt, p, knob_source):
             "opening": (f"size/theta + {p.open_delta_weight:g} delta" if p.flags & 0x8
                         else "size/theta"),
             "theta": p.theta, "eps": p.softening, "dt": dt, "G": p.g,
-            "lbits": p.lbits, "bucket": p.bucket, "group_size": p.group_size or 32,
+            "lbits": p.lbits, "key_bits": 3 * p.lbits, "layers": p.lbits + 1,
+            "bucket": p.bucket, "group_size": p.group_size or 32,
             "block_warps": p.block_warps or 4, "sort_variant": p.sort_variant,
             "open_delta_weight": p.open_delta_weight, "far_ratio": p.far_ratio,
             "walk_frontier": p.walk_frontier,
@@ -643,8 +771,8 @@ def config_dict(args, desc, n, dt, p, knob_source):
             "parallelism": "replicas (one independent system per GPU)"}
 
 
-def main():
-    args = parse()
+def main(argv=None):
+    args = parse(argv)
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         if rank != 0:
@@ -659,9 +787,13 @@ def main():
         dist.init_process_group("nccl")
     r = run_ours(args, world, rank, local)
     if rank == 0:
+        extra = None
+        if not args.no_extras and args.n is None and args.workload in ("c5", "c4"):
+            extra = extras(args)
         cpu = None
         if not args.no_cpu:
             cpu = cpu_run(args, r["pm"], r["vr"], r["sizes"], r["p"], r["dt"], args.cpu_seconds)
+        group = WORKLOADS[args.workload].preset != "reference" and args.walk == "group"
         line = {
             "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -672,21 +804,20 @@ def main():
             "e2e": r["e2e"], "gpu_launches": r["launches"],
             "roofline": {"kernel": ("traverse_ref_kernel"
                                     if WORKLOADS[args.workload].preset == "reference"
-                                    else "traverse_group_kernel" if args.walk == "group"
+                                    else "group_eval_kernel" if group
                                     else "traverse_phys_kernel"),
                          "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",
                          "frac": r["achieved"] / r["fp32_peak"],
-                         "traffic": NCU_TRAVERSAL_DRAM_BYTES.get((args.workload, args.form,
-                                                                   args.walk)),
+                         "traffic": NCU_EVAL_DRAM_BYTES.get((args.workload, args.form,
+                                                             r["p"].lbits)),
                          "flops_per_launch": r["flops"],
-                         "interactions_per_s": r["interactions"] / (r["trav_ms"] * 1e-3),
-                         "launch_ms": r["trav_ms"],
+                         "interactions_per_s": r["interactions"] / (r["kernel_ms"] * 1e-3),
+                         "launch_ms": r["kernel_ms"],
+                         "walk_kernel_ms": r["walk_ms"], "traversal_ms": r["trav_ms"],
                          "peak_source": f"2 x 128 FP32 lanes x SMs x sm_max_mhz ({r['peak_src']} peaks file)"},
             "cpu_baseline": cpu, "clocks": r["clocks"],
-            "error_vs_fp64_direct": None if r["err"] is None else {
-                "median": float(np.median(r["err"])), "p99": float(np.percentile(r["err"], 99)),
-                "samples": int(len(r["err"]))},
+            "error_vs_fp64_direct": r["err"],
             "interactions_per_particle": r["interactions"] / r["n"],
             "cell_interactions_per_particle": r["cell_inter"] / r["n"],
             "far_interactions_per_particle": r["far_inter"] / r["n"],
@@ -694,8 +825,9 @@ def main():
             "node_visits_per_particle": r["visits"] / r["n"],
             "stages_ms": r["stages"], "stage_roofline_hbm": r["stage_roofline"],
             "sort_roofline": r["sort_roofline"], "layer_counts": r["counts"],
-            "systems_one_at_a_time": r["one_at_a_time"],
         }
+        if extra:
+            line["extras"] = extra
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -282,6 +282,12 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
  * cell_interactions above). */
 int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions);
 
+/* Device times of the two kernels of the last group-walk traversal made by
+ * a stage call (astro_traverse; graph-replayed steps are not timed): the
+ * walk that builds the interaction lists and the evaluation that sums them
+ * (CUDA events on the context's stream; waits for them). */
+int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms);
+
 /* FP64 direct-sum accelerations (G, eps as the context's PHYSICAL params) of
  * the sampled particles against all particles of their own system, computed
  * on the device from the current positions. acc3 holds 3 doubles per sample. */
@@ -383,6 +389,13 @@ int astro_get_stream(astro_ctx* ctx, void** stream);
  * astro_autotune: target 1e-3, 1,024 samples. */
 int astro_autotune(astro_ctx* ctx, const char* path);
 int astro_autotune_ex(astro_ctx* ctx, const char* path, float target, uint32_t samples);
+/* astro_autotune_ex holding the knobs of `keep` (ASTRO_TUNE_KEEP_* bits) at
+ * the context's values, e.g. the tree depth a workload is quoted at. */
+#define ASTRO_TUNE_KEEP_LBITS 0x1u
+#define ASTRO_TUNE_KEEP_GROUP_SIZE 0x2u
+#define ASTRO_TUNE_KEEP_ACCURACY 0x4u  /* open_delta_weight and far_ratio */
+int astro_autotune_keep(astro_ctx* ctx, const char* path, float target, uint32_t samples,
+                        uint32_t keep);
 
 const char* astro_last_error(const astro_ctx* ctx);
 const char* astro_version(void);
