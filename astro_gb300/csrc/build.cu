@@ -416,15 +416,31 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
     if (kMode == 0) {
         const uint32_t sum_end = (j + 1 < u0) ? pe : u0;
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        // Stars (type 0): colours summed, positions averaged (Octree.metal:85-99).
+        float4 ec = make_float4(0.f, 0.f, 0.f, 0.f), en = ec;
+        uint32_t suns = 0;
         for (uint32_t i = pb; i < sum_end; ++i) {
-            const float4 q = a.pos[a.perm[i]];
+            const uint32_t pi = a.perm[i];
+            const float4 q = a.pos[pi];
             m = __fadd_rn(m, q.w);
             sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
             sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
             sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
+            if (a.node_ecol && a.types[pi] == 0u) {
+                const float4 c = a.colors[pi];
+                ec = make_float4(__fadd_rn(ec.x, c.x), __fadd_rn(ec.y, c.y), __fadd_rn(ec.z, c.z),
+                                 __fadd_rn(ec.w, c.w));
+                en = make_float4(__fadd_rn(en.x, q.x), __fadd_rn(en.y, q.y), __fadd_rn(en.z, q.z), 0.f);
+                ++suns;
+            }
         }
         if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
         else cm.w = m;
+        if (a.node_ecol) {
+            const float ns = fmaxf((float)suns, 1e-9f);
+            a.node_ecol[j] = ec;
+            a.node_ecen[j] = make_float4(__fdiv_rn(en.x, ns), __fdiv_rn(en.y, ns), __fdiv_rn(en.z, ns), 0.f);
+        }
     } else if (kMode == 1) {
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
         for (uint32_t i = pb; i < pe; ++i) {
@@ -536,6 +552,32 @@ __device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32
         }
         if (m > 0.f) cm = make_float4(__fdiv_rn(sx, m), __fdiv_rn(sy, m), __fdiv_rn(sz, m), m);
         else cm.w = m;
+        if (a.node_ecol) {
+            // Children whose emitted colour has alpha > 0: colours summed,
+            // centres averaged over those children (Octree.metal:155-178).
+            float4 ec = make_float4(0.f, 0.f, 0.f, 0.f), en = ec;
+            uint32_t suns = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                if (k < nch) {
+                    const float4 c = ld_l2(a.node_ecol + cb + k);
+                    if (c.w > 0.f) {
+                        const float4 e = ld_l2(a.node_ecen + cb + k);
+                        ec = make_float4(__fadd_rn(ec.x, c.x), __fadd_rn(ec.y, c.y),
+                                         __fadd_rn(ec.z, c.z), __fadd_rn(ec.w, c.w));
+                        en = make_float4(__fadd_rn(en.x, e.x), __fadd_rn(en.y, e.y),
+                                         __fadd_rn(en.z, e.z), 0.f);
+                        ++suns;
+                    }
+                }
+            }
+            if (suns > 0) {
+                const float ns = (float)suns;
+                en = make_float4(__fdiv_rn(en.x, ns), __fdiv_rn(en.y, ns), __fdiv_rn(en.z, ns), 0.f);
+            }
+            a.node_ecol[node] = ec;
+            a.node_ecen[node] = en;
+        }
     } else if (nch == 1) {
         // One child (most nodes of the lower layers): every sum is the
         // child's (0 + s is exact, and no sum is -0 since all start at +0),
@@ -806,6 +848,8 @@ __global__ void scatter_by_id_kernel(const T* __restrict__ src, const uint32_t* 
 __global__ void readback_nodes_kernel(const float4* __restrict__ node_cm,
                                       const uint4* __restrict__ node_rng,
                                       const uint64_t* __restrict__ node_key,
+                                      const float4* __restrict__ node_ecol,
+                                      const float4* __restrict__ node_ecen,
                                       const uint32_t* __restrict__ layer_count, uint32_t l,
                                       uint32_t layer_offset, uint32_t first_in_layer,
                                       uint32_t count, OctreeNode* __restrict__ out) {
@@ -826,6 +870,16 @@ __global__ void readback_nodes_kernel(const float4* __restrict__ node_cm,
         o.centerOfMass[2] = cm.z;
         o.totalMass = cm.w;
         o.layer = l;
+        if (node_ecol) {
+            const float4 ec = node_ecol[node], en = node_ecen[node];
+            o.emittedColor[0] = ec.x;
+            o.emittedColor[1] = ec.y;
+            o.emittedColor[2] = ec.z;
+            o.emittedColor[3] = ec.w;
+            o.emittedColorCenter[0] = en.x;
+            o.emittedColorCenter[1] = en.y;
+            o.emittedColorCenter[2] = en.z;
+        }
         if (l > 0) {
             const uint4 r = node_rng[node];
             for (uint32_t c = 0; c < 8 && r.x + c < r.y; ++c) o.children[c] = r.x + c;
@@ -1132,12 +1186,13 @@ cudaError_t launch_scatter_f4(const float4* src, const uint32_t* ids, float4* ds
 }
 
 cudaError_t launch_readback_nodes(const float4* cm, const uint4* rng, const uint64_t* key,
+                                  const float4* ecol, const float4* ecen,
                                   const uint32_t* layer_count, uint32_t l, uint32_t layer_offset,
                                   uint32_t first_in_layer, uint32_t count, OctreeNode* out,
                                   cudaStream_t st) {
     if (count == 0) return cudaSuccess;
     readback_nodes_kernel<<<blocks_for(count, 128), 128, 0, st>>>(
-        cm, rng, key, layer_count, l, layer_offset, first_in_layer, count, out);
+        cm, rng, key, ecol, ecen, layer_count, l, layer_offset, first_in_layer, count, out);
     return cudaGetLastError();
 }
 

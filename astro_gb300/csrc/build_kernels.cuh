@@ -45,6 +45,13 @@ struct AggArgs {
     float* node_qyz;       // Qyz
     uint2* groups;         // particle ranges of the group walk
     uint32_t* group_count;
+    // REFERENCE: star colours (ColorType colour of type-0 particles) summed
+    // into each node's emittedColor and averaged into emittedColorCenter
+    // (Octree.metal:75-106,147-187); NULL node_ecol = not computed.
+    const float4* colors;  // upload order
+    const uint32_t* types; // upload order
+    float4* node_ecol;     // emittedColor
+    float4* node_ecen;     // emittedColorCenter (w unused)
     uint32_t n;
     uint32_t lbits;
     uint32_t want_quad;
@@ -176,7 +183,10 @@ cudaError_t launch_scatter_u64(const uint64_t* src, const uint32_t* ids, uint64_
                                cudaStream_t st);
 cudaError_t launch_scatter_f4(const float4* src, const uint32_t* ids, float4* dst, uint32_t n,
                               cudaStream_t st);
+// ecol/ecen: emitted colours and their centres (NULL: zero, as in the
+// PHYSICAL preset).
 cudaError_t launch_readback_nodes(const float4* cm, const uint4* rng, const uint64_t* key,
+                                  const float4* ecol, const float4* ecen,
                                   const uint32_t* layer_count, uint32_t l, uint32_t layer_offset,
                                   uint32_t first_in_layer, uint32_t count, OctreeNode* out,
                                   cudaStream_t st);

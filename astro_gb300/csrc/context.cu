@@ -134,11 +134,17 @@ int ensure_tree(astro_ctx* ctx, uint64_t capacity) {
     dev_free(ctx->node_parent);
     dev_free(ctx->node_arrive);
     dev_free(ctx->node_crit2);
+    dev_free(ctx->node_ecol);
+    dev_free(ctx->node_ecen);
     dev_free(ctx->node_q);
     dev_free(ctx->node_qyz);
     ctx->tree_capacity = 0;
     const uint64_t cap = capacity;
     CK(dev_alloc(&ctx->node_crit2, cap));
+    if (!is_phys(ctx)) {
+        CK(dev_alloc(&ctx->node_ecol, cap));
+        CK(dev_alloc(&ctx->node_ecen, cap));
+    }
     CK(dev_alloc(&ctx->node_q, cap));
     CK(dev_alloc(&ctx->node_qyz, cap));
     CK(dev_alloc(&ctx->node_cm, cap));
@@ -308,6 +314,12 @@ int stage_build(astro_ctx* ctx) {
     a.node_qyz = ctx->node_qyz;
     a.groups = ctx->groups;
     a.group_count = ctx->counters + 2;
+    if (!is_phys(ctx)) {
+        a.colors = ctx->colors;
+        a.types = ctx->types;
+        a.node_ecol = ctx->node_ecol;
+        a.node_ecen = ctx->node_ecen;
+    }
     a.n = count;
     a.lbits = ctx->lbits;
     a.want_quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) ? 1u : 0u;
@@ -651,6 +663,8 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->node_parent);
     dev_free(ctx->node_arrive);
     dev_free(ctx->node_crit2);
+    dev_free(ctx->node_ecol);
+    dev_free(ctx->node_ecen);
     dev_free(ctx->node_q);
     dev_free(ctx->node_qyz);
     dev_free(ctx->groups);
@@ -968,6 +982,7 @@ int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t
         const uint64_t layer_end = (uint64_t)ctx->layers.offset[l] + ctx->layers.size[l];
         const uint64_t m = std::min<uint64_t>({chunk, first + count - pos, layer_end - pos});
         CK(astro::launch_readback_nodes(ctx->node_cm, ctx->node_rng, ctx->node_key,
+                                        ctx->node_ecol, ctx->node_ecen,
                                         ctx->layer_count, l, ctx->layers.offset[l],
                                         (uint32_t)(pos - ctx->layers.offset[l]), (uint32_t)m, d_out,
                                         st));

@@ -134,6 +134,8 @@ struct astro_ctx {
     uint32_t* node_parent = nullptr;
     uint32_t* node_arrive = nullptr;
     float* node_crit2 = nullptr;      // opening radius^2 per node
+    float4* node_ecol = nullptr;      // REFERENCE: emittedColor per node
+    float4* node_ecen = nullptr;      // REFERENCE: emittedColorCenter per node
     float4* node_q = nullptr;         // quadrupole Qxx, Qyy, Qxy, Qxz
     float* node_qyz = nullptr;        // quadrupole Qyz
     uint2* groups = nullptr;          // group-walk particle ranges (<= n)

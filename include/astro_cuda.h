@@ -76,8 +76,10 @@ typedef struct ASTRO_ALIGN16 ColorType {
     uint32_t _pad[3];
 } ColorType;
 
-/* bridge.h:47-65 — 128-byte node. emittedColor / emittedColorCenter are kept
- * for layout compatibility; no kernel on the step reads them. */
+/* bridge.h:47-65 — 128-byte node. emittedColor / emittedColorCenter: in the
+ * REFERENCE preset the stars' (type 0) colours summed and their positions
+ * averaged, leaf by leaf, then over children with emitted alpha > 0
+ * (Octree.metal:75-106,147-187); zero in the PHYSICAL preset. */
 typedef struct ASTRO_ALIGN16 OctreeNode {
     uint64_t mortonCode;        /* @0   */
     uint64_t _pad0;             /* @8   */

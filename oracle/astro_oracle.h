@@ -46,6 +46,8 @@ typedef struct oracle_outputs {
     uint64_t node_visits;
     uint64_t far_nodes;        /* group walk: expansions formed (group x far node) */
     uint64_t far_interactions; /* accepted nodes evaluated through them, per particle */
+    const uint64_t* nodes_index; /* PHYSICAL: nodes holds only these nodes_count slots, */
+    uint64_t nodes_count;        /* in this order (NULL: every slot) */
 } oracle_outputs;
 
 /* Number of OpenMP threads used by the oracle (<=0: all). Returns the count in effect. */

@@ -37,6 +37,7 @@ class Outputs(ctypes.Structure):
         ("layer_counts", c_void_p), ("layer_sizes", c_void_p), ("layer_offsets", c_void_p),
         ("nodes", c_void_p), ("acc4", c_void_p), ("interactions", c_uint64),
         ("node_visits", c_uint64), ("far_nodes", c_uint64), ("far_interactions", c_uint64),
+        ("nodes_index", c_void_p), ("nodes_count", c_uint64),
     ]
 
 
@@ -165,13 +166,22 @@ def phys_capacity(sizes, lbits: int) -> int:
     return cap
 
 
-def phys_run(params, pm, vr, sizes=None, dt=1e-3, steps=1, split_passes=0, want_pos64=False):
-    """PHYSICAL preset: `steps` steps in place over one or several systems."""
+def phys_run(params, pm, vr, sizes=None, dt=1e-3, steps=1, split_passes=0, want_pos64=False,
+             nodes=None):
+    """PHYSICAL preset: `steps` steps in place over one or several systems.
+    nodes (an array of node slots) returns only those slots, in that order
+    (for trees too large to hold whole as OctreeNode records)."""
     n = len(pm)
     sizes = [n] if sizes is None else [int(s) for s in sizes]
     layers = params.lbits + 1
     cap = phys_capacity(sizes, params.lbits)
-    bufs, out = _outputs(n, n, layers, cap)
+    if nodes is not None:
+        index = np.ascontiguousarray(nodes, np.uint64)
+        bufs, out = _outputs(n, n, layers, len(index))
+        bufs["_nodes_index"] = index
+        out.nodes_index, out.nodes_count = _p(index), len(index)
+    else:
+        bufs, out = _outputs(n, n, layers, cap)
     sz = np.ascontiguousarray(sizes, np.uint32)
     pos64 = np.zeros((n, 3), np.float64) if want_pos64 else None
     r = lib().oracle_phys_run(ctypes.addressof(params), _p(pm), _p(vr), n, _p(sz), len(sz), dt,

@@ -827,24 +827,26 @@ struct PhysState {
         out->far_interactions = far_interactions;
         out->node_visits = visits;
         if (out->nodes) {
-            for (uint64_t i = 0; i < capacity; ++i) {
+            // Every slot, or the listed ones (nodes_index) in their order.
+            const uint64_t count = out->nodes_index ? out->nodes_count : capacity;
+            for (uint64_t i = 0; i < count; ++i) {
+                const uint64_t slot = out->nodes_index ? out->nodes_index[i] : i;
                 OctreeNode& o = out->nodes[i];
                 std::memset(&o, 0, sizeof(o));
                 o.mortonCode = kInvalidCode;
                 for (int c = 0; c < 8; ++c) o.children[c] = kInvalidChild;
+                uint32_t l = 0;
+                while (l + 1 < layers && slot >= offsets[l + 1]) ++l;
+                if (slot >= capacity || slot < offsets[l] || slot - offsets[l] >= counts[l]) continue;
+                const uint32_t node = (uint32_t)slot;
+                o.mortonCode = sorted[pbeg[node]] >> (3u * l);
+                for (int a = 0; a < 3; ++a) o.centerOfMass[a] = cm[4ull * node + a];
+                o.totalMass = cm[4ull * node + 3];
+                o.layer = l;
+                if (l > 0)
+                    for (uint32_t c = cbeg[node], q = 0; c < cend[node] && q < 8; ++c, ++q)
+                        o.children[q] = c;
             }
-            for (uint32_t l = 0; l < layers; ++l)
-                for (uint32_t k = 0; k < counts[l]; ++k) {
-                    uint32_t node = offsets[l] + k;
-                    OctreeNode& o = out->nodes[node];
-                    o.mortonCode = sorted[pbeg[node]] >> (3u * l);
-                    for (int a = 0; a < 3; ++a) o.centerOfMass[a] = cm[4ull * node + a];
-                    o.totalMass = cm[4ull * node + 3];
-                    o.layer = l;
-                    if (l > 0)
-                        for (uint32_t c = cbeg[node], q = 0; c < cend[node] && q < 8; ++c, ++q)
-                            o.children[q] = c;
-                }
         }
     }
 };

@@ -252,6 +252,7 @@ struct RefFrame {
     std::vector<OctreeNode> nodes;
     std::vector<float> force;  // float3 with 16-byte stride
     std::vector<uint32_t> types;
+    std::vector<float> colors;  // ColorType colours (4 per particle; zero when none given)
 
     void init(const astro_params& prm, uint32_t n_, uint32_t n_tree_, const ColorType* ct) {
         p = prm;
@@ -273,6 +274,10 @@ struct RefFrame {
         force.assign(4ull * n, 0.0f);
         types.resize(n);
         for (uint32_t i = 0; i < n; ++i) types[i] = ct ? ct[i].type : (i < n_tree ? 1u : 2u);
+        colors.assign(4ull * n, 0.0f);
+        if (ct)
+            for (uint32_t i = 0; i < n; ++i)
+                for (int a = 0; a < 4; ++a) colors[4ull * i + a] = ct[i].color[a];
     }
 
     // countUniqueMortonCodes, Renderer.swift:570-625: clears, markUniques
@@ -321,12 +326,20 @@ struct RefFrame {
             uint32_t start = unique_idx[gid];
             uint32_t end = (gid + 1 < num_unique) ? unique_idx[gid + 1] : num_unique;
             float cx = 0.0f, cy = 0.0f, cz = 0.0f, mass = 0.0f;
+            float ec[4] = {0.0f, 0.0f, 0.0f, 0.0f}, en[3] = {0.0f, 0.0f, 0.0f};
+            uint32_t suns = 0;
             for (uint32_t i = start; i < end; ++i) {
-                const PositionMass& s = pm[sorted_idx[i]];
+                const uint32_t si = sorted_idx[i];
+                const PositionMass& s = pm[si];
                 mass += s.mass;
                 cx += s.position[0] * s.mass;
                 cy += s.position[1] * s.mass;
                 cz += s.position[2] * s.mass;
+                if (types[si] == 0) {  // Octree.metal:85-89
+                    for (int a = 0; a < 4; ++a) ec[a] += colors[4ull * si + a];
+                    for (int a = 0; a < 3; ++a) en[a] += s.position[a];
+                    ++suns;
+                }
             }
             OctreeNode node = empty_node();
             node.mortonCode = sorted_codes[start];
@@ -336,6 +349,10 @@ struct RefFrame {
                 node.centerOfMass[2] = cz / mass;
             }
             node.totalMass = mass;
+            // Octree.metal:93-98: the centre divides by max(suns, 1e-9).
+            const float suns_safe = std::max((float)suns, 1e-9f);
+            for (int a = 0; a < 4; ++a) node.emittedColor[a] = ec[a];
+            for (int a = 0; a < 3; ++a) node.emittedColorCenter[a] = en[a] / suns_safe;
             node.layer = 0;
             nodes[gid] = node;
             unsorted_codes[gid] = node.mortonCode;
@@ -354,6 +371,8 @@ struct RefFrame {
             uint32_t start = unique_idx[gid];
             uint32_t end = (gid + 1 < num_unique) ? unique_idx[gid + 1] : child_count;
             float cx = 0.0f, cy = 0.0f, cz = 0.0f, mass = 0.0f;
+            float ec[4] = {0.0f, 0.0f, 0.0f, 0.0f}, en[3] = {0.0f, 0.0f, 0.0f};
+            uint32_t suns = 0;
             uint32_t children[8];
             for (int i = 0; i < 8; ++i) children[i] = kInvalidChild;
             int child_n = 0;
@@ -364,6 +383,11 @@ struct RefFrame {
                 cx += c.centerOfMass[0] * c.totalMass;
                 cy += c.centerOfMass[1] * c.totalMass;
                 cz += c.centerOfMass[2] * c.totalMass;
+                if (c.emittedColor[3] > 0.0f) {  // Octree.metal:155-159
+                    for (int a = 0; a < 4; ++a) ec[a] += c.emittedColor[a];
+                    for (int a = 0; a < 3; ++a) en[a] += c.emittedColorCenter[a];
+                    ++suns;
+                }
                 if (child_n < 8) children[child_n++] = node_index;
             }
             OctreeNode node = empty_node();
@@ -374,6 +398,11 @@ struct RefFrame {
                 node.centerOfMass[2] = cz / mass;
             }
             node.totalMass = mass;
+            // Octree.metal:171-177: the centre is averaged over the children
+            // that emit.
+            for (int a = 0; a < 4; ++a) node.emittedColor[a] = ec[a];
+            for (int a = 0; a < 3; ++a)
+                node.emittedColorCenter[a] = suns > 0 ? en[a] / (float)suns : en[a];
             node.layer = layer;
             for (int i = 0; i < 8; ++i) node.children[i] = children[i];
             nodes[output_offset + gid] = node;

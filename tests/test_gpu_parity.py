@@ -125,6 +125,10 @@ def test_reference_scene_bit_exact(ag, oracle):
     pm_o, vr_o = pm.copy(), vr.copy()
     ref = oracle.ref_run(p, pm_o, vr_o, ct, n_tree=205, dt=1.0 / 60, steps=3, split_passes=64)
     assert_tree_equal(out, ref)
+    # The stars light the tree: emitted colours and centres are part of the
+    # compared records (Octree.metal:75-106,147-187).
+    assert (out["nodes"]["emittedColor"][:, 3] > 0).sum() >= 5
+    assert np.array_equal(out["nodes"]["emittedColorCenter"], ref["nodes"]["emittedColorCenter"])
     assert np.array_equal(out["acc4"], ref["acc4"])
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o)
 

@@ -465,3 +465,47 @@ def test_far_ratio_one_particle_groups_and_systems(oracle, native):
     # rho = 0 for a single particle: the expansion is the node's field itself.
     rel = np.linalg.norm(a1 - a0, axis=1) / np.maximum(np.linalg.norm(a0, axis=1), 1e-30)
     assert rel.max() < 1e-5
+
+
+def test_emitted_colour_known_answers(oracle):
+    """emittedColor / emittedColorCenter (Octree.metal:75-106,147-187): a leaf
+    sums its stars' colours and averages their positions (dividing by
+    max(stars, 1e-9), so a starless leaf has centre 0); an internal node sums
+    the colours of the children whose emitted alpha is above 0 and averages
+    those children's centres."""
+    # Two stars in one leaf cell (quantised x 1,000,000 and 1,000,100), one
+    # planet in another, and a third star in the other half of the cube.
+    pm, vr = particles([(0.0, 0.0, 0.0), (100.0, 0.0, 0.0), (500000.0, 0.0, 0.0),
+                        (-600000.0, 0.0, 0.0)])
+    ct = np.zeros(4, L.COLOR_TYPE)
+    ct["color"] = [(1.0, 0.5, 0.25, 1.0), (0.5, 0.5, 0.5, 1.0), (0.9, 0.9, 0.9, 1.0),
+                   (0.25, 0.25, 0.25, 0.5)]
+    ct["type"] = [0, 0, 1, 0]
+    out = oracle.ref_run(ref_params(), pm, vr, ct, n_tree=4, dt=0.0, steps=1, split_passes=64)
+    nodes = out["nodes"]
+    leaves = nodes[:out["layer_counts"][0]]
+    by_mass = {int(round(float(l["totalMass"]))): l for l in leaves}
+    pair = [l for l in leaves if l["totalMass"] == 2.0][0]
+    assert np.array_equal(pair["emittedColor"], np.float32([1.5, 1.0, 0.75, 2.0]))
+    assert np.array_equal(pair["emittedColorCenter"], np.float32([50.0, 0.0, 0.0]))
+    # The planet's leaf sorts last and, by the last-leaf range of
+    # aggregateLeafNodes (Octree.metal:71), sums nothing: no mass, no light.
+    planet = leaves[-1]
+    assert planet["totalMass"] == 0.0
+    assert not planet["emittedColor"].any() and not planet["emittedColorCenter"].any()
+    lone = [l for l in leaves if l["centerOfMass"][0] == -600000.0][0]
+    assert np.array_equal(lone["emittedColor"], np.float32([0.25, 0.25, 0.25, 0.5]))
+    assert np.array_equal(lone["emittedColorCenter"], np.float32([-600000.0, 0.0, 0.0]))
+    assert len(by_mass) == 3
+    root = nodes[out["layer_offsets"][-1]]
+    assert np.array_equal(root["emittedColor"], np.float32([1.75, 1.25, 1.0, 2.5]))
+    # Where the stars' branches meet, two children emit and their centres
+    # (50 and -600000) are averaged; above it one child carries that on.
+    def emitting(node):
+        return [c for c in node["children"] if c != L.INVALID_CHILD
+                and nodes[c]["emittedColor"][3] > 0]
+
+    joins = [nd for nd in nodes[out["layer_counts"][0]:] if len(emitting(nd)) == 2]
+    assert len(joins) == 1
+    assert np.array_equal(joins[0]["emittedColorCenter"], np.float32([-299975.0, 0.0, 0.0]))
+    assert np.array_equal(root["emittedColorCenter"], np.float32([-299975.0, 0.0, 0.0]))
