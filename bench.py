@@ -21,9 +21,11 @@ metric's comparison on the batching workload (256 Plummer systems): plain
 FP32 batched, precision + batched, and the systems stepped one at a time.
 `--impl reference` times the CPU restatement of the reference kernels
 (oracle/, OpenMP over all host cores) on the same workload within a time
-budget. Under torchrun every rank runs an independent replica (the
-single-system step does not shard); rank 0 prints the line with the max
-time over ranks.
+budget. Under torchrun every rank runs an independent replica of a
+single-system workload (one tree per step must be globally consistent), and
+the batching workload's systems are sharded over the ranks in contiguous
+ranges balanced by N log N (astro_gb300.shard; no exchange); rank 0 prints
+the line with the max time over ranks.
 """
 from __future__ import annotations
 
@@ -414,7 +416,21 @@ def run_ours(args, world, rank, local):
     w = workload(args)
     desc, dt = w.description, w.dt
     pm, vr, sizes = w.make()
+    total_n = len(pm)
+    sharded = bool(sizes) and world > 1
+    if sharded:
+        # The batching form shards by system: this rank steps its contiguous
+        # range of systems (balanced by N log N), with no exchange.
+        from astro_gb300 import shard
+
+        if len(sizes) < world:
+            raise SystemExit("fewer systems than ranks")
+        rng = shard.partition_systems(sizes, world)[rank]
+        a, b = shard.particle_range(sizes, rng)
+        pm, vr, sizes = pm[a:b].copy(), vr[a:b].copy(), sizes[rng[0]:rng[1]]
     n = len(pm)
+    # Particles all ranks advance per step: replicas each step a whole copy.
+    job_n = total_n if sharded else n * world
     form = L.FORM_PRECISION if args.form == "precision" else L.FORM_PLAIN
     p, knob_source = make_params(args, L, ag.default_params)
     nsys = len(sizes) if sizes else 1
@@ -450,7 +466,7 @@ def run_ours(args, world, rank, local):
     barrier(world)
     t_ms = sum(step_ms)
     t_ms_max = reduce_max(t_ms, world)
-    value = n * args.steps * world / (t_ms_max * 1e-3)
+    value = job_n * args.steps / (t_ms_max * 1e-3)
 
     # One instrumented step: per-stage times.
     stages = {}
@@ -548,7 +564,7 @@ def run_ours(args, world, rank, local):
             sim.download(hpm, hvr)
         te = time.perf_counter() - t0
         te = reduce_max(te, world)
-        e2e = {"value": n * args.steps * world / te, "unit": UNIT,
+        e2e = {"value": job_n * args.steps / te, "unit": UNIT,
                "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 64 * n,
                "ms_per_step": te * 1e3 / args.steps}
 
@@ -556,7 +572,8 @@ def run_ours(args, world, rank, local):
     sim.close()
     del flush
     torch.cuda.empty_cache()
-    return dict(n=n, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value, t_ms=t_ms_max,
+    return dict(n=n, sharded=sharded, desc=desc, dt=dt, p=p, knob_source=knob_source, value=value,
+                t_ms=t_ms_max,
                 wall=wall, step_ms=step_ms, stages=stages, interactions=interactions,
                 visits=visits, cell_inter=cell_inter, flops=flops, far_nodes=far_nodes,
                 far_inter=far_inter, counts=[int(c) for c in counts], trav_ms=trav,
@@ -752,7 +769,7 @@ def run_reference(args):
     }
 
 
-def config_dict(args, desc, n, dt, p, knob_source):
+def config_dict(args, desc, n, dt, p, knob_source, shards=1):
     walk = ("per-particle (the reference's)" if p.preset == 0
             else "per-particle" if p.flags & 0x20 else "group")
     return {"workload": f"{args.workload}: {desc}", "n": n,
@@ -768,7 +785,9 @@ def config_dict(args, desc, n, dt, p, knob_source):
             "walk_frontier": p.walk_frontier,
             "knob_source": knob_source,
             "l2": "flushed (256 MB write) before every timed step",
-            "parallelism": "replicas (one independent system per GPU)"}
+            "parallelism": (f"systems sharded over {shards} GPUs (contiguous ranges balanced by "
+                            "N log N, no exchange; n is rank 0's share)" if shards > 1
+                            else "replicas (one independent system per GPU)")}
 
 
 def main(argv=None):
@@ -797,10 +816,12 @@ def main(argv=None):
         line = {
             "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": r["t_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": r["t_ms"] / args.steps, "higher_is_better": True,
+            "scaling": "strong" if r["sharded"] else "weak",
             "vs_baseline": None, "dtype": "f32" if args.form == "plain" else "f32+f64",
             "data": "synthetic (seeded, Philox4x32-10)",
-            "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"], r["knob_source"]),
+            "config": config_dict(args, r["desc"], r["n"], r["dt"], r["p"], r["knob_source"],
+                                  world if r["sharded"] else 1),
             "e2e": r["e2e"], "gpu_launches": r["launches"],
             "roofline": {"kernel": ("traverse_ref_kernel"
                                     if WORKLOADS[args.workload].preset == "reference"
