@@ -130,3 +130,44 @@ def test_reupload_in_the_same_layout_reuses_the_step(ag):
             fresh.draw(1e-3, 3)
             want = fresh.download()
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+
+
+@pytest.mark.parametrize("case", ["plain", "batched", "reference"])
+def test_oracle_started_from_a_state_file_equals_the_gpu_continuation(ag, oracle, tmp_path, case):
+    """The file carries the whole state: the CPU restatement started from the
+    particles read out of a saved file (in their saved slot order) steps to
+    what the GPU context loaded from that file steps to, bit for bit
+    (IEEE-exact traversal), so a field that saving and loading both got
+    wrong would show. The precision form is left out: its FP64 master
+    positions are state the restatement does not take as input."""
+    L = ag.layouts
+    p, d, sizes, dt = _setup(ag, case)
+    if p.preset == L.PRESET_PHYSICAL:
+        p = p.replace(flags=p.flags | L.FLAG_IEEE_EXACT)
+    path = tmp_path / "state.bin"
+    sim = _open(ag, p, d, sizes)
+    sim.draw(dt, 3)
+    sim.save_state(path, step=3, time=3 * dt)
+    sim.close()
+    hdr, ss, pm_s, vr_s, ids, types, pos64 = L.read_state(path)
+    assert pos64 is None and hdr.n == len(d["pm"])
+
+    sim2, step, _ = ag.Simulation.load_state(path)
+    with sim2:
+        assert step == 3
+        sim2.draw(dt, 2)
+        pm_g, vr_g = sim2.download()
+        acc_g = sim2.read_accel()
+
+    if p.preset == L.PRESET_REFERENCE:
+        ct = np.zeros(hdr.n, L.COLOR_TYPE)
+        ct["type"] = types
+        ref = oracle.ref_run(p, pm_s, vr_s, ct, n_tree=hdr.n_tree, dt=dt, steps=2,
+                             split_passes=64)
+    else:
+        ref = oracle.phys_run(p, pm_s, vr_s, sizes=[int(s) for s in ss] if hdr.nsys > 1 else None,
+                              dt=dt, steps=2)
+    # GPU results come back in upload order; the file's slots map to it by ids.
+    assert np.array_equal(pm_g[ids], pm_s)
+    assert np.array_equal(vr_g[ids], vr_s)
+    assert np.array_equal(acc_g[ids], ref["acc4"])
