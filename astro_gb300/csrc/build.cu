@@ -893,7 +893,8 @@ __global__ void readback_nodes_kernel(const float4* __restrict__ node_cm,
 constexpr int kDirectSamples = 8;
 
 // Softened FP64 direct sum for sampled particles (error reference). Each
-// block takes kDirectSamples samples; threads stride over the particles.
+// block takes kDirectSamples samples and one slice of their particles
+// (threads stride over it) and adds its partial sums to the output.
 __global__ __launch_bounds__(256) void direct_sum_f64_kernel(DirectArgs a) {
     __shared__ double s_red[8][kDirectSamples][3];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -919,7 +920,11 @@ __global__ __launch_bounds__(256) void direct_sum_f64_kernel(DirectArgs a) {
             acc[s][c] = 0.0;
         }
     }
-    for (uint32_t j = glo + tid; j < ghi; j += blockDim.x) {
+    // blockIdx.y takes one of gridDim.y slices of the samples' particle range.
+    const uint32_t span = ghi > glo ? ghi - glo : 0u;
+    const uint32_t per = (span + gridDim.y - 1) / gridDim.y;
+    const uint32_t jb = glo + blockIdx.y * per, je = min(ghi, jb + per);
+    for (uint32_t j = jb + tid; j < je; j += blockDim.x) {
         const float4 q = a.pos[j];
         double xj[3];
         for (int c = 0; c < 3; ++c)
@@ -947,7 +952,7 @@ __global__ __launch_bounds__(256) void direct_sum_f64_kernel(DirectArgs a) {
         const int s = tid / 3, c = tid % 3;
         double v = 0;
         for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) v += s_red[w][s][c];
-        if (first + s < a.n_sample) a.out[3ull * (first + s) + c] = v;
+        if (first + s < a.n_sample) atomicAdd(&a.out[3ull * (first + s) + c], v);
     }
 }
 
@@ -1198,7 +1203,13 @@ cudaError_t launch_readback_nodes(const float4* cm, const uint4* rng, const uint
 
 cudaError_t launch_direct_sum(const DirectArgs& a, cudaStream_t st) {
     if (a.n_sample == 0) return cudaSuccess;
-    direct_sum_f64_kernel<<<blocks_for(a.n_sample, kDirectSamples), 256, 0, st>>>(a);
+    // Sample blocks times slices of the particle range (each slice adds its
+    // partial sums), about 1,024 blocks in all, slices of at least 8,192.
+    const uint32_t xb = blocks_for(a.n_sample, kDirectSamples);
+    const uint32_t ys = std::max(1u, std::min((1024u + xb - 1) / xb, (a.n + 8191u) / 8192u));
+    cudaError_t e = cudaMemsetAsync(a.out, 0, 24ull * a.n_sample, st);
+    if (e != cudaSuccess) return e;
+    direct_sum_f64_kernel<<<dim3(xb, ys), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
