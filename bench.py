@@ -585,18 +585,20 @@ def run_ours(args, world, rank, local):
                 vr=vr, stage_roofline=stage_roofline, sort_roofline=sort_roofline)
 
 
-def run_variant(torch, args, workload_name, form, lbits, steps, warmup, error_samples=512):
+def run_variant(torch, args, workload_name, form, lbits, steps, warmup, error_samples=512,
+                theta=None):
     """Another configuration of the line: workload `workload_name` in `form`
-    at tree depth `lbits` (None: tuned), its tuned knobs, `steps` timed
-    steps after an L2 flush each. Returns its throughput, step time, knobs
-    and error (PHYSICAL workloads)."""
+    at tree depth `lbits` (None: tuned), its tuned knobs, opening angle
+    `theta` (None: the line's), `steps` timed steps after an L2 flush each.
+    Returns its throughput, step time, knobs and error (PHYSICAL workloads)."""
     import astro_gb300 as ag
     from astro_gb300 import layouts as L
 
     va = argparse.Namespace(**{**vars(args), "workload": workload_name, "form": form,
                                "lbits": lbits, "n": None, "bucket": None, "warps": None,
                                "group_size": None, "sort_variant": None, "delta_weight": None,
-                               "far_ratio": None, "walk_frontier": None})
+                               "far_ratio": None, "walk_frontier": None,
+                               "theta": args.theta if theta is None else theta})
     w = WORKLOADS[workload_name]
     pm, vr, sizes = w.make()
     n = len(pm)
@@ -616,6 +618,7 @@ def run_variant(torch, args, workload_name, form, lbits, steps, warmup, error_sa
         err = error_vs_direct(sim, n, w.seed, error_samples)
         k, _ = knobs(va)
         return {"workload": f"{workload_name}: {w.description}", "form": form, "lbits": p.lbits,
+                "theta": p.theta,
                 "value": n * steps / (sum(ms) * 1e-3), "unit": UNIT,
                 "ms_per_step": float(np.mean(ms)), "steps": steps, "knobs": k,
                 "knob_source": source, "error_vs_fp64_direct": err}
@@ -673,9 +676,10 @@ def one_at_a_time(torch, args, steps, warmup):
 
 
 def extras(args):
-    """The default line's other configurations: C5 at lbits 21 (63-bit keys)
-    and in the precision form, and the batching workload plain batched,
-    precision + batched and one system at a time."""
+    """The default line's other configurations: C5 at lbits 21 (63-bit keys),
+    in the precision form and at opening angles 0.3, 0.5 and 1.0, and the
+    batching workload plain batched, precision + batched and one system at
+    a time."""
     import torch
 
     k = max(3, args.steps // 4)
@@ -683,6 +687,9 @@ def extras(args):
     if args.workload == "c5" and args.form == "plain":
         out["c5_lbits21"] = run_variant(torch, args, "c5", "plain", 21, k, args.warmup)
         out["c5_precision"] = run_variant(torch, args, "c5", "precision", 6, k, args.warmup)
+        # The configuration's opening-angle sweep at lbits 6, the line's knobs.
+        out["c5_theta_sweep"] = [run_variant(torch, args, "c5", "plain", 6, 3, 1, theta=t)
+                                 for t in (0.3, 0.5, 1.0)]
     plain = run_variant(torch, args, "c4", "plain", None, k, args.warmup)
     prec = run_variant(torch, args, "c4", "precision", None, k, args.warmup)
     alone = one_at_a_time(torch, args, max(2, k // 2), args.warmup)
