@@ -318,6 +318,7 @@ __global__ __launch_bounds__(kTopoThreads) void topology_kernel(TopoArgs a) {
             if (lev[k] >= l) {
                 const uint32_t node = s_off[l] + rank;
                 a.pbeg[node] = i;
+                a.node_key[node] = key[k] >> (3u * l);
                 if (l > 0) a.cbeg[node] = s_off[l - 1] + idx_below;
                 idx_below = rank;
                 if (l < lbits) pending = node;
@@ -345,16 +346,25 @@ __device__ __forceinline__ void quad_add(float q[5], float m, float dx, float dy
 
 // Opening radius^2 of a node: (size / theta + w |com - cell centre|)^2, the
 // cell found from the node's key prefix in its system's box.
-__device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t key, uint32_t l, float4 cm) {
-    const uint32_t s = (uint32_t)(key >> (3u * a.lbits));
+// Geometric centre (x, y, z) and edge (w) of the layer-l cell of a node;
+// node_key = first key >> 3l: the system above bit 3 (lbits - l), the
+// cell's code below it (3 (lbits - l) <= 63).
+__device__ __forceinline__ float4 cell_box(const AggArgs& a, uint64_t node_key, uint32_t l) {
+    const uint32_t below = 3u * (a.lbits - l);
+    const uint32_t s = (uint32_t)(node_key >> below);
     const SysInfo& si = a.sys[s];
-    const uint64_t mask = (3u * a.lbits >= 64) ? ~0ull : ((1ull << (3u * a.lbits)) - 1ull);
-    const uint64_t code = (key & mask) >> (3u * l);
+    const uint64_t code = node_key & ((1ull << below) - 1ull);
     const float size = __fmul_rn(si.ext, exp2_exact((int)l - (int)a.lbits));
     const float half = __fmul_rn(0.5f, size);
-    const float cx = __fadd_rn(si.lo[0], __fmul_rn((float)(2u * compact3_21(code) + 1u), half));
-    const float cy = __fadd_rn(si.lo[1], __fmul_rn((float)(2u * compact3_21(code >> 1) + 1u), half));
-    const float cz = __fadd_rn(si.lo[2], __fmul_rn((float)(2u * compact3_21(code >> 2) + 1u), half));
+    return make_float4(__fadd_rn(si.lo[0], __fmul_rn((float)(2u * compact3_21(code) + 1u), half)),
+                       __fadd_rn(si.lo[1], __fmul_rn((float)(2u * compact3_21(code >> 1) + 1u), half)),
+                       __fadd_rn(si.lo[2], __fmul_rn((float)(2u * compact3_21(code >> 2) + 1u), half)),
+                       size);
+}
+
+__device__ __forceinline__ float node_crit2(const AggArgs& a, uint64_t node_key, uint32_t l, float4 cm) {
+    const float4 box = cell_box(a, node_key, l);
+    const float size = box.w, cx = box.x, cy = box.y, cz = box.z;
     const float dx = __fsub_rn(cm.x, cx), dy = __fsub_rn(cm.y, cy), dz = __fsub_rn(cm.z, cz);
     const float dd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     const float crit = __fadd_rn(__fdiv_rn(size, a.theta), __fmul_rn(a.delta_weight, __fsqrt_rn(dd)));
@@ -399,6 +409,55 @@ __device__ __forceinline__ uint32_t reserve_groups(uint32_t* counter, uint32_t c
     return __shfl_sync(mask, base, leader) + prefix;
 }
 
+// Mass moments of a leaf's particles about a point c (the cell's centre):
+// first moments D = sum m d and second moments S = sum m d d^T, d = x - c,
+// in FP32, each product and sum rounded separately. quadrupole() shifts them
+// to the centre of mass e + c (e = com - c): P = S - e D^T - D e^T + M e e^T,
+// Q = 3 P - tr(P) I (traceless), components Qxx, Qyy, Qxy, Qxz, Qyz. The
+// particles lie inside the cell, so |d| is at most its half diagonal and
+// the shift loses little; one read of the particles then gives the sums and
+// the quadrupole together (a second pass about the centre of mass re-read
+// them from DRAM once the position array had streamed through L2).
+struct CellMoments {
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    float sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+    __device__ __forceinline__ void add(float4 q, float4 c) {
+        const float ux = __fsub_rn(q.x, c.x), uy = __fsub_rn(q.y, c.y), uz = __fsub_rn(q.z, c.z);
+        const float tx = __fmul_rn(q.w, ux), ty = __fmul_rn(q.w, uy), tz = __fmul_rn(q.w, uz);
+        dx = __fadd_rn(dx, tx);
+        dy = __fadd_rn(dy, ty);
+        dz = __fadd_rn(dz, tz);
+        sxx = __fadd_rn(sxx, __fmul_rn(tx, ux));
+        syy = __fadd_rn(syy, __fmul_rn(ty, uy));
+        szz = __fadd_rn(szz, __fmul_rn(tz, uz));
+        sxy = __fadd_rn(sxy, __fmul_rn(tx, uy));
+        sxz = __fadd_rn(sxz, __fmul_rn(tx, uz));
+        syz = __fadd_rn(syz, __fmul_rn(ty, uz));
+    }
+    // P_ab = ((S_ab - e_a D_b) - e_b D_a) + e_a (M e_b)
+    __device__ __forceinline__ static float shifted(float s, float ea, float eb, float da, float db,
+                                                    float m) {
+        return __fadd_rn(__fsub_rn(__fsub_rn(s, __fmul_rn(ea, db)), __fmul_rn(eb, da)),
+                         __fmul_rn(ea, __fmul_rn(m, eb)));
+    }
+    __device__ __forceinline__ void quadrupole(float4 cm, float4 c, float q[5]) const {
+        const float ex = __fsub_rn(cm.x, c.x), ey = __fsub_rn(cm.y, c.y), ez = __fsub_rn(cm.z, c.z);
+        const float m = cm.w;
+        const float pxx = shifted(sxx, ex, ex, dx, dx, m);
+        const float pyy = shifted(syy, ey, ey, dy, dy, m);
+        const float pzz = shifted(szz, ez, ez, dz, dz, m);
+        const float pxy = shifted(sxy, ex, ey, dx, dy, m);
+        const float pxz = shifted(sxz, ex, ez, dx, dz, m);
+        const float pyz = shifted(syz, ey, ez, dy, dz, m);
+        const float tr = __fadd_rn(__fadd_rn(pxx, pyy), pzz);
+        q[0] = __fsub_rn(__fmul_rn(3.0f, pxx), tr);
+        q[1] = __fsub_rn(__fmul_rn(3.0f, pyy), tr);
+        q[2] = __fmul_rn(3.0f, pxy);
+        q[3] = __fmul_rn(3.0f, pxz);
+        q[4] = __fmul_rn(3.0f, pyz);
+    }
+};
+
 // aggregateLeafNodes (Octree.metal:53-117), one thread per leaf.
 // kMode 0 (REFERENCE): state in upload order, gathered through perm; FP32
 //   sums of m and x*m in sorted order; the last leaf sums [start, numUnique)
@@ -406,12 +465,17 @@ __device__ __forceinline__ uint32_t reserve_groups(uint32_t* counter, uint32_t c
 // kMode 1 (PHYSICAL plain): state already in sorted order; raw FP32 sums.
 // kMode 2 (PHYSICAL precision): FP64 sums of m and m*x over the FP32
 //   positions relative to the system origin.
-template <int kMode>
-__device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j, uint32_t u0) {
+template <int kMode, bool kQuad>
+__device__ __forceinline__ void aggregate_leaf_node_q(const AggArgs& a, uint32_t j, uint32_t u0) {
     const uint32_t pb = a.pbeg[j];
     const uint32_t pe = (j + 1 < u0) ? a.pbeg[j + 1] : a.n;
-    const uint64_t key = a.sorted_keys[pb];
-    a.node_key[j] = key;
+    // PHYSICAL quadrupole in the same read of the particles as the sums:
+    // moments about the cell's centre, shifted to the centre of mass after.
+    uint64_t node_key = 0;
+    float4 box = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (kMode != 0 && (kQuad || a.want_delta)) node_key = a.node_key[j];
+    if (kQuad) box = cell_box(a, node_key, 0);
+    CellMoments mom;
     float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
     if (kMode == 0) {
         const uint32_t sum_end = (j + 1 < u0) ? pe : u0;
@@ -449,6 +513,7 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
             sx = __fadd_rn(sx, __fmul_rn(q.w, q.x));
             sy = __fadd_rn(sy, __fmul_rn(q.w, q.y));
             sz = __fadd_rn(sz, __fmul_rn(q.w, q.z));
+            if (kQuad) mom.add(q, box);
         }
         reinterpret_cast<float4*>(a.node_sum)[j] = make_float4(sx, sy, sz, m);
         cm = com_from_sums(sx, sy, sz, m);
@@ -465,6 +530,7 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
             sx = __fma_rn(mi, (double)q.x, sx);
             sy = __fma_rn(mi, (double)q.y, sy);
             sz = __fma_rn(mi, (double)q.z, sz);
+            if (kQuad) mom.add(q, box);
         }
         reinterpret_cast<double4*>(a.node_sum)[j] = make_double4(sx, sy, sz, m);
         if (pe - pb == 1 && m >= 1.17549435e-38) {
@@ -480,16 +546,13 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
     a.node_cm[j] = cm;
     a.node_rng[j] = make_uint4(0u, 0u, pb, pe);
     if (kMode != 0) {
-        if (a.want_quad) {
-            float q[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-            for (uint32_t i = pb; i < pe; ++i) {
-                const float4 x = a.pos[i];
-                quad_add(q, x.w, __fsub_rn(x.x, cm.x), __fsub_rn(x.y, cm.y), __fsub_rn(x.z, cm.z));
-            }
+        if (kQuad) {
+            float q[5];
+            mom.quadrupole(cm, box, q);
             a.node_q[j] = make_float4(q[0], q[1], q[2], q[3]);
             a.node_qyz[j] = q[4];
         }
-        if (a.want_delta) a.node_crit2[j] = node_crit2(a, key, 0, cm);
+        if (a.want_delta) a.node_crit2[j] = node_crit2(a, node_key, 0, cm);
         // A leaf holding more than one group is cut into group-sized chunks.
         const uint32_t gs = a.group_size;
         const uint32_t c = pe - pb > gs ? (pe - pb + gs - 1u) / gs : 0u;
@@ -497,6 +560,12 @@ __device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j
         for (uint32_t i = 0; i < c; ++i)
             a.groups[slot + i] = make_uint2(pb + i * gs, min(pb + (i + 1u) * gs, pe));
     }
+}
+
+template <int kMode>
+__device__ __forceinline__ void aggregate_leaf_node(const AggArgs& a, uint32_t j, uint32_t u0) {
+    if (kMode != 0 && a.want_quad) aggregate_leaf_node_q<kMode, true>(a, j, u0);
+    else aggregate_leaf_node_q<kMode, false>(a, j, u0);
 }
 
 // aggregateNodes (Octree.metal:120-202) for node j of layer l (one thread).
@@ -528,8 +597,6 @@ __device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32
     const uint32_t pe = (j + 1 < u) ? a.pbeg[node + 1] : a.n;
     if (ce - cb > 8u) atomicOr(a.err, kErrBadLayer);
     const uint32_t nch = min(ce - cb, 8u);
-    const uint64_t key = a.sorted_keys[pb];
-    a.node_key[node] = key >> (3u * l);
     float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 ccm[8];  // children's centres of mass (modes 0 and quadrupoles)
     const bool need_ccm = kMode == 0 || (kMode != 0 && a.want_quad);
@@ -653,7 +720,7 @@ __device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32
             a.node_q[node] = make_float4(q[0], q[1], q[2], q[3]);
             a.node_qyz[node] = q[4];
         }
-        if (a.want_delta) a.node_crit2[node] = node_crit2(a, key, l, cm);
+        if (a.want_delta) a.node_crit2[node] = node_crit2(a, a.node_key[node], l, cm);
         // Groups: a node over the group size packs runs of consecutive
         // small children (greedy, in child order); a small top-layer node is
         // a group by itself.

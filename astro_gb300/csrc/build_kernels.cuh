@@ -17,6 +17,7 @@ struct TopoArgs {
     uint32_t* pbeg;
     uint32_t* cbeg;
     uint32_t* parent;    // per node: the node one layer up holding it (kNoParent at the top)
+    uint64_t* node_key;  // per node: its first particle's key >> 3 * layer
     uint32_t* layer_count;
     uint32_t* lookback;  // [ntiles][32] status words
     uint32_t* tile_counter;
@@ -24,7 +25,6 @@ struct TopoArgs {
 };
 
 struct AggArgs {
-    const uint64_t* sorted_keys;
     const uint32_t* perm;      // REFERENCE: sorted slot -> upload index
     const float4* pos;         // REFERENCE: upload order; PHYSICAL: sorted order (the
                                // precision form's FP32 frame relative to the origin)
@@ -142,8 +142,12 @@ struct TraverseArgs {
     uint32_t* lists;          // group walk: list pool, lists_blocks blocks
     uint32_t* list_next;      // group walk: next block of each block's chain
     uint32_t lists_blocks;    // pool size in blocks
-    uint32_t* lists_used;     // pool bump counter (blocks handed out)
+    uint32_t* lists_used;     // pool bump counter (blocks handed out, past the end
+                              // when the pool is too small: the demand)
     uint32_t* eval_queue;     // queue of the group evaluation kernel
+    uint32_t* frontier_need;  // group walk: largest frontier (words) a walk wanted
+                              // past frontier_cap (atomicMax)
+    uint32_t* evals_done;     // group walk: evaluations that ran (one per launch)
     uint32_t nsys;
     float far2;               // group walk: far_ratio^2 (0: no far nodes)
     uint32_t group_chunk;     // group walk: groups visited in scrambled chunks of this

@@ -81,7 +81,7 @@ enum DeviceError : uint32_t {
     kErrLookbackTimeout = 1u << 0,  // a decoupled look-back wait gave up
     kErrStackOverflow = 1u << 1,    // a traversal stack bound was hit
     kErrBadLayer = 1u << 2,
-    kErrFrontier = 1u << 3,         // a group walk's frontier exceeded its buffer
+    kErrFrontier = 1u << 3,         // a group walk's frontier or list pool was too small
 };
 
 // Bounded spin for decoupled look-back: after this many polls the waiting

@@ -21,6 +21,7 @@
 #include "build_kernels.cuh"
 #include "common.cuh"
 #include "internal.h"
+#include "../../include/astro_cuda_testing.h"
 
 using astro::Chunk;
 using astro::LayerTable;
@@ -166,11 +167,60 @@ int ensure_x64(astro_ctx* ctx) {
     return ASTRO_OK;
 }
 
-// Read and clear the device error word (waits for the stream).
+int ensure_frontier(astro_ctx* ctx);
+void drop_graph(astro_ctx* ctx);
+int launch_steps(astro_ctx* ctx, float dt, uint32_t nsteps);
+
+// After a group walk ran out of frontier or list room (the evaluation then
+// skipped, leaving the state as it was): sizes the buffers from what the
+// walk asked for (pool blocks handed out, largest frontier wanted; both
+// under-counted when the frontier was cut short, hence at least doubled)
+// and clears the error word and the counters. The stream is idle.
+int grow_walk_buffers(astro_ctx* ctx, uint32_t* evals_done) {
+    uint32_t c[3] = {0, 0, 0};  // pool blocks handed out, frontier wanted, evaluations run
+    CK(cudaMemcpy(c, ctx->counters + 4, sizeof(c), cudaMemcpyDeviceToHost));
+    *evals_done = c[2];
+    const size_t slack = (size_t)astro::group_walk_warps() * 16;
+    if (c[0] >= ctx->lists_blocks)
+        ctx->lists_blocks_want = std::max<size_t>(2 * ctx->lists_blocks, (size_t)c[0] + c[0] / 4 + slack);
+    // Frontier sizes stay multiples of 4 words: the run form stores 8-byte
+    // runs in both buffers of a warp, the second starting frontier_cap words in.
+    const uint64_t fmax = std::max<uint64_t>(64, 2ull * ctx->max_n);
+    if (c[1] > ctx->frontier_cap || c[0] < ctx->lists_blocks) {
+        const uint64_t want = std::min<uint64_t>(
+            fmax, std::max<uint64_t>(2ull * ctx->frontier_cap, (uint64_t)c[1] + c[1] / 4));
+        ctx->frontier_cap = (uint32_t)((want + 3) & ~3ull);
+    }
+    ctx->lists_blocks_want = std::min<size_t>(ctx->lists_blocks_want, 0xFFFFFF00ull);
+    CK(cudaMemset(ctx->counters + 4, 0, sizeof(c)));
+    CK(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
+    return ensure_frontier(ctx);
+}
+
+// Read and clear the device error word (waits for the stream). Steps whose
+// group walk ran out of room were not evaluated; they run again with
+// larger buffers, so the state continues exactly as without the overflow.
 int check_device(astro_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     uint32_t err = 0;
     CK(cudaMemcpy(&err, ctx->err, sizeof(err), cudaMemcpyDeviceToHost));
+    for (int attempt = 0; err == astro::kErrFrontier && ctx->pending_steps > 0 && attempt < 16;
+         ++attempt) {
+        uint32_t done = 0;
+        int r = grow_walk_buffers(ctx, &done);
+        if (r != ASTRO_OK) return r;
+        const uint32_t left = ctx->pending_steps - std::min(done, ctx->pending_steps);
+        ctx->pending_steps = 0;
+        ctx->walk_reruns += left;
+        drop_graph(ctx);
+        if ((r = launch_steps(ctx, ctx->pending_dt, left)) != ASTRO_OK) return r;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(&err, ctx->err, sizeof(err), cudaMemcpyDeviceToHost));
+    }
+    if (ctx->pending_steps > 0) {
+        ctx->pending_steps = 0;
+        CK(cudaMemset(ctx->counters + 6, 0, sizeof(uint32_t)));
+    }
     if (err) {
         CK(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
         if (err & astro::kErrLookbackTimeout)
@@ -223,8 +273,12 @@ int ensure_frontier(astro_ctx* ctx) {
         CK(dev_alloc(&ctx->frontier, words));
         ctx->frontier_words = words;
     }
-    const size_t blocks = astro::group_list_blocks(
-        ctx->max_n, ctx->p.group_size ? ctx->p.group_size : astro::kDefaultGroupSize);
+    const size_t estimate =
+        ctx->walk_estimate_off
+            ? 0
+            : astro::group_list_blocks(ctx->max_n, ctx->p.group_size ? ctx->p.group_size
+                                                                     : astro::kDefaultGroupSize);
+    const size_t blocks = std::max(estimate, ctx->lists_blocks_want);
     if (blocks > ctx->lists_blocks) {
         dev_free(ctx->lists);
         dev_free(ctx->list_next);
@@ -287,6 +341,7 @@ int stage_build(astro_ctx* ctx) {
     t.pbeg = ctx->node_pbeg;
     t.cbeg = ctx->node_cbeg;
     t.parent = ctx->node_parent;
+    t.node_key = ctx->node_key;
     t.layer_count = ctx->layer_count;
     t.lookback = ctx->topo_lookback;
     t.tile_counter = ctx->counters;
@@ -295,7 +350,6 @@ int stage_build(astro_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->counters, 0, sizeof(uint32_t), st));
     CK(astro::launch_topology(t, st));
     astro::AggArgs a{};
-    a.sorted_keys = ctx->sorted_keys;
     a.perm = ctx->perm;
     a.pos = is_phys(ctx) ? ctx->pos[1] : ctx->pos[0];
     a.sys = ctx->sys;
@@ -384,6 +438,8 @@ astro::TraverseArgs traverse_args(astro_ctx* ctx, float dt, bool integrate) {
     a.lists_blocks = (uint32_t)ctx->lists_blocks;
     a.eval_queue = ctx->counters + 3;
     a.lists_used = ctx->counters + 4;
+    a.frontier_need = ctx->counters + 5;
+    a.evals_done = ctx->counters + 6;
     a.nsys = ctx->nsys;
     if (is_phys(ctx)) {
         a.eps2 = ctx->p.softening * ctx->p.softening;
@@ -488,6 +544,48 @@ int capture_step(astro_ctx* ctx, float dt) {
     return ASTRO_OK;
 }
 
+// Launches nsteps whole steps (graph replays unless ASTRO_FLAG_NO_GRAPH);
+// group-walk steps are counted until the next device check.
+int launch_steps(astro_ctx* ctx, float dt, uint32_t nsteps) {
+    if (nsteps == 0) return ASTRO_OK;
+    if (group_walk(ctx)) {
+        ctx->pending_steps += nsteps;
+        ctx->pending_dt = dt;
+    }
+    int r;
+    if ((ctx->p.flags & ASTRO_FLAG_NO_GRAPH) != 0) {
+        for (uint32_t s = 0; s < nsteps; ++s)
+            if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
+        return ASTRO_OK;
+    }
+    // The step is captured once per (upload, params, dt) and replayed.
+    if (!(ctx->graph_valid && ctx->graph_dt == dt))
+        if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
+    for (uint32_t s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    ctx->tree_valid = true;
+    return ASTRO_OK;
+}
+
+// A stage-call traversal whose walk ran out of room runs again at once with
+// larger buffers (the sorted state and the tree are still in place). Other
+// device errors stay in the error word for the next check.
+int settle_traverse(astro_ctx* ctx) {
+    for (int attempt = 0; attempt < 16; ++attempt) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        uint32_t err = 0;
+        CK(cudaMemcpy(&err, ctx->err, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err != astro::kErrFrontier) break;
+        uint32_t done = 0;
+        int r = grow_walk_buffers(ctx, &done);
+        if (r != ASTRO_OK) return r;
+        ctx->state_in_b = true;
+        ++ctx->walk_reruns;
+        if ((r = stage_traverse(ctx, 0.0f, false)) != ASTRO_OK) return r;
+    }
+    CK(cudaMemsetAsync(ctx->counters + 6, 0, sizeof(uint32_t), ctx->stream));
+    return ASTRO_OK;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ ABI --
@@ -564,7 +662,7 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
     ctx->max_sys = max_systems;
     // A walk frontier holds at most one layer's nodes of one system (node
     // list) or one run per opened node (runs, two words each): 2 max_n words.
-    ctx->frontier_cap = (uint32_t)std::min<uint64_t>(16384, std::max<uint64_t>(64, 2ull * max_n));
+    ctx->frontier_cap = (uint32_t)std::min<uint64_t>(16384, std::max<uint64_t>(64, 4ull * ((max_n + 1) / 2)));
     auto cleanup = [&](int code) {
         astro_destroy(ctx);
         return code;
@@ -883,7 +981,10 @@ int astro_build(astro_ctx* ctx) {
 int astro_traverse(astro_ctx* ctx) {
     NEED_UPLOAD();
     drop_graph(ctx);
-    return stage_traverse(ctx, 0.0f, false);
+    int r;
+    if (ctx->pending_steps > 0 && (r = check_device(ctx)) != ASTRO_OK) return r;
+    if ((r = stage_traverse(ctx, 0.0f, false)) != ASTRO_OK) return r;
+    return group_walk(ctx) ? settle_traverse(ctx) : ASTRO_OK;
 }
 int astro_integrate(astro_ctx* ctx, float dt) {
     NEED_UPLOAD();
@@ -895,18 +996,11 @@ int astro_step(astro_ctx* ctx, float dt, uint32_t nsteps) {
     NEED_UPLOAD();
     if (!std::isfinite(dt)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "dt must be finite");
     if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "step called between sort and traverse");
+    // Steps still unchecked run again at their own dt if they overflowed.
     int r;
-    if ((ctx->p.flags & ASTRO_FLAG_NO_GRAPH) != 0) {
-        for (uint32_t s = 0; s < nsteps; ++s)
-            if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
-        return ASTRO_OK;
-    }
-    // The step is captured once per (upload, params, dt) and replayed.
-    if (nsteps > 0 && !(ctx->graph_valid && ctx->graph_dt == dt))
-        if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
-    for (uint32_t s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-    if (nsteps > 0) ctx->tree_valid = true;
-    return ASTRO_OK;
+    if (ctx->pending_steps > 0 && ctx->pending_dt != dt && (r = check_device(ctx)) != ASTRO_OK)
+        return r;
+    return launch_steps(ctx, dt, nsteps);
 }
 
 int astro_synchronize(astro_ctx* ctx) {
@@ -1342,6 +1436,42 @@ int astro_load_state(const char* path, uint32_t max_n, astro_ctx** out, uint64_t
     if (step) *step = h.step;
     if (time) *time = h.time;
     *out = ctx;
+    return ASTRO_OK;
+}
+
+int astro_read_walk_buffers(astro_ctx* ctx, uint64_t* list_blocks, uint32_t* frontier_cap,
+                            uint64_t* reruns) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    int r = check_device(ctx);
+    if (r != ASTRO_OK) return r;
+    if (list_blocks) *list_blocks = ctx->lists_blocks;
+    if (frontier_cap) *frontier_cap = ctx->frontier_cap;
+    if (reruns) *reruns = ctx->walk_reruns;
+    return ASTRO_OK;
+}
+
+int astro_test_walk_capacity(astro_ctx* ctx, uint64_t set_blocks, uint32_t set_frontier_cap) {
+    if (!ctx || (set_frontier_cap != 0 && (set_frontier_cap < 2 || set_frontier_cap % 2 != 0)) ||
+        set_blocks > 0xFFFFFF00ull)
+        return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!is_phys(ctx)) return fail(ctx, ASTRO_ERR_STATE, "the group walk is PHYSICAL only");
+    int r = check_device(ctx);
+    if (r != ASTRO_OK) return r;
+    drop_graph(ctx);
+    ctx->walk_estimate_off = true;
+    if (set_blocks) {
+        dev_free(ctx->lists);
+        dev_free(ctx->list_next);
+        ctx->lists_blocks = 0;
+        ctx->lists_blocks_want = set_blocks;
+    }
+    if (set_frontier_cap) {
+        dev_free(ctx->frontier);
+        ctx->frontier_words = 0;
+        ctx->frontier_cap = set_frontier_cap;
+    }
+    if ((r = ensure_frontier(ctx)) != ASTRO_OK) return r;
+    CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }
 

@@ -146,6 +146,11 @@ struct astro_ctx {
     uint32_t* lists = nullptr;        // group walk: list pool
     uint32_t* list_next = nullptr;    // group walk: block chain links
     size_t lists_blocks = 0;
+    size_t lists_blocks_want = 0;     // group walk: pool size a walk asked for
+    bool walk_estimate_off = false;   // group walk: size the pool by demand only (test hook)
+    uint64_t walk_reruns = 0;         // steps / traversals run again after a walk overflow
+    uint32_t pending_steps = 0;       // steps launched since the last device check
+    float pending_dt = 0.f;           // their time step
     uint32_t* layer_count = nullptr;  // device [ASTRO_MAX_LAYERS]
 
     // Systems.

@@ -96,8 +96,11 @@ struct BlockCache {
 
 // Appends the items of the lanes in `mask` (in lane order) to list L, whose
 // items are kWords words each (this lane's words w0, w1). A full block is
-// chained to a new one; if the pool is exhausted the error bit is set and
-// `failed` drops the group's lists. `mask` is warp-uniform.
+// chained to a new one. Blocks numbered past the pool's end are not
+// written: the walk goes on counting them (the pool counter ends at the
+// demand), `failed` marks the group and the error bit makes the evaluation
+// skip, so the host can grow the pool and run the traversal again.
+// `mask` is warp-uniform.
 template <uint32_t kWords>
 __device__ __forceinline__ void list_append(const TraverseArgs& a, ListTail& L, BlockCache& bc,
                                             uint32_t mask, uint32_t lane, uint32_t lt, uint32_t w0,
@@ -110,28 +113,25 @@ __device__ __forceinline__ void list_append(const TraverseArgs& a, ListTail& L, 
             uint32_t b = 0;
             if (lane == 0) b = atomicAdd(a.lists_used, kBlockBatch);
             b = __shfl_sync(kFullMask, b, 0);
-            if ((uint64_t)b + kBlockBatch > (uint64_t)a.lists_blocks) {
-                if (lane == 0) atomicOr(a.err, kErrFrontier);
-                failed = true;
-                return kNoBlock;
-            }
             bc.next = b;
             bc.end = b + kBlockBatch;
         }
-        return bc.next++;
+        const uint32_t blk = bc.next++;
+        if (blk >= a.lists_blocks && !failed) {
+            if (lane == 0) atomicOr(a.err, kErrFrontier);
+            failed = true;
+        }
+        return blk;
     };
-    if (failed) return;
     if (L.blk == kNoBlock) {
         L.blk = L.first = alloc();
         L.fill = 0;
-        if (failed) return;
     }
     uint32_t b = L.blk, slot = L.fill + rank;
     const uint32_t room = kCap - L.fill;
     if (cnt > room) {
         const uint32_t nb = alloc();
-        if (failed) return;
-        if (lane == 0) a.list_next[L.blk] = nb;
+        if (lane == 0 && L.blk < a.lists_blocks && nb < a.lists_blocks) a.list_next[L.blk] = nb;
         if (rank >= room) {
             b = nb;
             slot = rank - room;
@@ -142,7 +142,7 @@ __device__ __forceinline__ void list_append(const TraverseArgs& a, ListTail& L, 
         L.fill += cnt;
     }
     L.count += cnt;
-    if ((mask >> lane) & 1u) {
+    if (((mask >> lane) & 1u) && b < a.lists_blocks) {
         uint32_t* dst = a.lists + (size_t)b * kListBlockWords + slot * kWords;
         if constexpr (kWords == 2) *reinterpret_cast<uint2*>(dst) = make_uint2(w0, w1);
         else *dst = w0;
@@ -296,6 +296,7 @@ __global__ __launch_bounds__(kWalkWarps * 32, kWalkWarpsPerSm / kWalkWarps) void
                                 nnext += __popc(bopen);
                             } else if (lane == 0) {
                                 atomicOr(a.err, kErrFrontier);
+                                atomicMax(a.frontier_need, 2u * (nnext + __popc(bopen)));
                             }
                         }
                     }
@@ -336,6 +337,7 @@ __global__ __launch_bounds__(kWalkWarps * 32, kWalkWarpsPerSm / kWalkWarps) void
                         nnext += total;
                     } else if (lane == 0) {
                         atomicOr(a.err, kErrFrontier);
+                        atomicMax(a.frontier_need, nnext + total);
                     }
                 }
                 __syncwarp();
@@ -888,6 +890,11 @@ __global__ ASTRO_EVAL_BOUNDS(kWarps) void group_eval_kernel(TraverseArgs a) {
     __shared__ float4 s_tile[kWarps][32];
     __shared__ uint32_t s_jdx[kWarps][32];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // A walk that ran out of frontier or list room left incomplete lists:
+    // nothing is evaluated or integrated (the state stays as it was) and
+    // the host runs the traversal again with larger buffers.
+    if (*reinterpret_cast<volatile const uint32_t*>(a.err) & kErrFrontier) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.evals_done, 1u);
     const uint32_t ngroups = *a.group_count;
     uint32_t inter = 0, cell_inter = 0, far_inter = 0;
     while (true) {

@@ -123,7 +123,10 @@ int Tuner::measure(const Knobs& k, Trial* t) {
     int r = apply(k);
     if (r != ASTRO_OK) return r;
     cudaStream_t st = ctx_->stream;
+    // Warm-up, checked: a walk that needs larger buffers gets them here,
+    // not inside the timed steps.
     if ((r = astro_step(ctx_, 0.0f, 3)) != ASTRO_OK) return r;
+    if ((r = astro_synchronize(ctx_)) != ASTRO_OK) return r;
     cudaEventRecord(ev_[0], st);
     if ((r = astro_step(ctx_, 0.0f, steps_)) != ASTRO_OK) return r;
     cudaEventRecord(ev_[1], st);

@@ -249,6 +249,14 @@ class Simulation:
         self._check(lib().astro_read_traverse_times(self._h, byref(w), byref(e)))
         return w.value, e.value
 
+    def walk_buffers(self) -> tuple[int, int, int]:
+        """(list pool blocks, frontier words per buffer, steps and
+        traversals run again since creation because a group walk had
+        outgrown its buffers). Waits for the context's stream."""
+        b, f, r = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
+        self._check(lib().astro_read_walk_buffers(self._h, byref(b), byref(f), byref(r)))
+        return b.value, f.value, r.value
+
     def direct_accel_f64(self, samples) -> np.ndarray:
         s = np.ascontiguousarray(samples, dtype=np.uint32)
         out = np.zeros((len(s), 3), np.float64)

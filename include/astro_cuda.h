@@ -290,6 +290,21 @@ int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_inte
  * (CUDA events on the context's stream; waits for them). */
 int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms);
 
+/* Group-walk buffers (PHYSICAL, group walk). The walk writes each group's
+ * interaction lists into a pool of 64-word blocks and walks the tree level
+ * by level through two frontier buffers per walk warp. A walk that needs
+ * more room than they have (small theta, large buckets) writes nothing past
+ * them and counts what it needs; its evaluation is skipped, leaving forces
+ * and particles as they were, and at the next check of the device
+ * (astro_synchronize, a readback) the buffers grow to the counted need and
+ * the skipped steps run again, so the results equal those of buffers large
+ * enough from the start. Stage calls (astro_traverse) do the same before
+ * returning. Reports the pool size in blocks, the frontier buffer size in
+ * words and the steps and traversals run again since astro_create (any
+ * pointer may be NULL). Waits for the context's stream. */
+int astro_read_walk_buffers(astro_ctx* ctx, uint64_t* list_blocks, uint32_t* frontier_cap,
+                            uint64_t* reruns);
+
 /* FP64 direct-sum accelerations (G, eps as the context's PHYSICAL params) of
  * the sampled particles against all particles of their own system, computed
  * on the device from the current positions. acc3 holds 3 doubles per sample. */

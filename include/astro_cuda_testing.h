@@ -28,6 +28,17 @@ int astro_test_sort_lookback_timeout(const uint64_t* d_input, uint64_t* d_output
                                      uint32_t spin_limit, void* d_temp, size_t temp_bytes,
                                      void* stream);
 
+/* Group-walk buffer sizes of a PHYSICAL context: set_blocks > 0 replaces
+ * the list pool with one of set_blocks 64-word blocks, set_frontier_cap > 0
+ * (even, at least 2) gives each walk warp's two frontier buffers that many
+ * words,
+ * and the size estimate taken from max_n and the group size is no longer
+ * applied, so that the next walks run out of room and the recovery (the
+ * evaluation skipped, buffers grown from the walk's demand, the steps run
+ * again) is exercised. astro_read_walk_buffers reports the sizes. Waits for
+ * the context's stream. */
+int astro_test_walk_capacity(astro_ctx* ctx, uint64_t set_blocks, uint32_t set_frontier_cap);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -4,11 +4,14 @@
  * and time the CUDA path. Nothing in the product (astro_gb300/, include/)
  * links, loads or calls this code.
  *
- * Parity status: the reference publishes no golden vectors, fixtures or
- * kernel tests (its tests are empty Xcode templates), and it cannot run here
- * (Swift + Metal on macOS). The restatement is pinned by the known-answer
- * tests in tests/test_oracle_kat.py and the committed fixtures under
- * tests/golden/, which were derived by hand from the reference source.
+ * Parity status: parity unpinned. The reference publishes no golden
+ * vectors, fixtures or kernel tests (its tests are empty Xcode templates),
+ * and it cannot run here (Swift + Metal on macOS), so nothing the reference
+ * holds or produces checks this restatement. It is checked only against the
+ * known-answer tests in tests/test_oracle_kat.py and the fixtures under
+ * tests/golden/, derived by hand from the reference source
+ * (tests/golden/make_golden.py), and the PHYSICAL preset against an FP64
+ * direct sum.
  *
  * Two presets (ASTRO_PRESET_* in include/astro_cuda.h):
  *   REFERENCE — every Metal kernel of the step restated as a loop over gid,

@@ -753,6 +753,18 @@ struct PhysState {
             for (int64_t kk = 0; kk < (int64_t)u; ++kk) {
                 uint32_t node = off + (uint32_t)kk;
                 const float* c = &cm[4ull * node];
+                const uint32_t s = sys_of[pbeg[node]];
+                // The node's cell: geometric centre and edge.
+                float center[3], size;
+                {
+                    uint64_t code = (sorted[pbeg[node]] & ((1ull << (3 * lbits)) - 1)) >> (3 * l);
+                    uint32_t cc[3] = {0, 0, 0};
+                    for (uint32_t b = 0; b < lbits - l; ++b)
+                        for (int a = 0; a < 3; ++a) cc[a] |= (uint32_t)((code >> (3 * b + a)) & 1) << b;
+                    size = std::ldexp(quant[s].ext, (int)l - (int)lbits);
+                    float half = 0.5f * size;
+                    for (int a = 0; a < 3; ++a) center[a] = quant[s].lo[a] + (float)(2 * cc[a] + 1) * half;
+                }
                 if (want_q) {
                     float q[5] = {0, 0, 0, 0, 0};
                     auto add = [&](float m, float dx, float dy, float dz) {
@@ -764,10 +776,37 @@ struct PhysState {
                         q[4] += m * (3 * dy * dz);
                     };
                     if (l == 0) {
+                        // A leaf: first and second mass moments about the
+                        // cell centre in one pass, shifted to the centre of
+                        // mass: P = S - e D^T - D e^T + M e e^T, e = com -
+                        // centre; Q = 3 P - tr(P) I.
+                        float d[3] = {0, 0, 0}, sm[6] = {0, 0, 0, 0, 0, 0};  // xx yy zz xy xz yz
                         for (uint32_t i = pbeg[node]; i < pend[node]; ++i) {
                             const float* x = &rel[4ull * i];
-                            add(x[3], x[0] - c[0], x[1] - c[1], x[2] - c[2]);
+                            const float u[3] = {x[0] - center[0], x[1] - center[1], x[2] - center[2]};
+                            const float t[3] = {x[3] * u[0], x[3] * u[1], x[3] * u[2]};
+                            for (int a = 0; a < 3; ++a) d[a] += t[a];
+                            sm[0] += t[0] * u[0];
+                            sm[1] += t[1] * u[1];
+                            sm[2] += t[2] * u[2];
+                            sm[3] += t[0] * u[1];
+                            sm[4] += t[0] * u[2];
+                            sm[5] += t[1] * u[2];
                         }
+                        const float e[3] = {c[0] - center[0], c[1] - center[1], c[2] - center[2]};
+                        const float mm = c[3];
+                        auto shifted = [&](float sab, int a, int b) {
+                            return ((sab - e[a] * d[b]) - e[b] * d[a]) + e[a] * (mm * e[b]);
+                        };
+                        const float pxx = shifted(sm[0], 0, 0), pyy = shifted(sm[1], 1, 1),
+                                    pzz = shifted(sm[2], 2, 2), pxy = shifted(sm[3], 0, 1),
+                                    pxz = shifted(sm[4], 0, 2), pyz = shifted(sm[5], 1, 2);
+                        const float tr = (pxx + pyy) + pzz;
+                        q[0] = 3.0f * pxx - tr;
+                        q[1] = 3.0f * pyy - tr;
+                        q[2] = 3.0f * pxy;
+                        q[3] = 3.0f * pxz;
+                        q[4] = 3.0f * pyz;
                     } else {
                         for (uint32_t ch = cbeg[node]; ch < cend[node]; ++ch) {
                             const float* cc = &cm[4ull * ch];
@@ -778,18 +817,8 @@ struct PhysState {
                     for (int a = 0; a < 5; ++a) quad[5ull * node + a] = q[a];
                 }
                 if (want_d) {
-                    uint32_t s = sys_of[pbeg[node]];
-                    uint64_t code = (sorted[pbeg[node]] & ((1ull << (3 * lbits)) - 1)) >> (3 * l);
-                    uint32_t cc[3] = {0, 0, 0};
-                    for (uint32_t b = 0; b < lbits - l; ++b)
-                        for (int a = 0; a < 3; ++a) cc[a] |= (uint32_t)((code >> (3 * b + a)) & 1) << b;
-                    float size = std::ldexp(quant[s].ext, (int)l - (int)lbits);
-                    float half = 0.5f * size;
                     float d[3];
-                    for (int a = 0; a < 3; ++a) {
-                        float center = quant[s].lo[a] + (float)(2 * cc[a] + 1) * half;
-                        d[a] = c[a] - center;
-                    }
+                    for (int a = 0; a < 3; ++a) d[a] = c[a] - center[a];
                     float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                     float crit = size / p.theta + p.open_delta_weight * std::sqrt(dd);
                     ncrit2[node] = crit * crit;
