@@ -14,7 +14,7 @@ The knobs are fields of astro_params that change speed, not physics:
   bucket        leaf tile size: an opened node holding <= bucket particles
                 is summed particle by particle
   sort_variant  radix sort pass kernel (items per thread / blocks per SM /
-                ranking / pipelined)
+                ranking / pipelined / lean)
   walk_frontier the group walk's frontier: runs of consecutive child nodes
                 or a list of node indices
 
@@ -84,7 +84,7 @@ def candidates(knob: str, n: int) -> list[int]:
     if knob == "block_warps":
         return [4, 8]
     if knob == "sort_variant":
-        return list(range(1, 10))
+        return list(range(1, 13))
     if knob == "walk_frontier":
         return [0, 1]
     if knob == "far_ratio":

@@ -134,15 +134,25 @@ __global__ __launch_bounds__(kThreads) void sort_histogram_kernel(
     }
 }
 
+// The tile in sorted order for the scatter: keys with their values, or
+// (lean passes) keys with the tile-local index of their value.
+template <int kItems, bool kLean>
+struct StageArrays {
+    uint64_t keys[kThreads * kItems];
+    uint32_t vals[kThreads * kItems];
+};
 template <int kItems>
+struct StageArrays<kItems, true> {
+    uint64_t keys[kThreads * kItems];
+    uint16_t src[kThreads * kItems];
+};
+
+template <int kItems, bool kLean = false>
 struct PassSmem {
     static constexpr int kTile = kThreads * kItems;
     union {
         uint32_t warp_hist[kWarps][kRadix];  // ranking: per-warp digit counters
-        struct {
-            uint64_t keys[kTile];
-            uint32_t vals[kTile];
-        } stage;                             // scatter: the tile in sorted order
+        StageArrays<kItems, kLean> stage;    // scatter: the tile in sorted order
     } u;
     uint32_t tile_start[kRadix];   // first slot of each digit inside the tile
     uint32_t global_base[kRadix];  // first output slot of each digit of this tile
@@ -150,18 +160,27 @@ struct PassSmem {
     uint32_t tile_id;
 };
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // One onesweep pass. kItems pairs per thread; kMatch ranks with
 // __match_any_sync and one shared atomic per distinct digit, otherwise with
-// per-bit ballots and per-warp counters.
-template <int kItems, int kMinBlocks, bool kMatch>
+// per-bit ballots and per-warp counters. kLean keeps no value in registers:
+// the tile's values are prefetched into L2 when the keys are loaded and
+// gathered by their tile-local index (staged as 16 bits beside the key) in
+// the scatter, so fewer registers and less shared memory let more blocks
+// share an SM.
+template <int kItems, int kMinBlocks, bool kMatch, bool kLean = false>
 __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
     const uint32_t* __restrict__ d_count, uint32_t n_est, const uint32_t* __restrict__ excl,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_counter, uint32_t shift,
     uint32_t digit_bits, uint32_t* __restrict__ err, uint32_t spin_limit) {
-    using Smem = PassSmem<kItems>;
+    using Smem = PassSmem<kItems, kLean>;
     constexpr int kTile = Smem::kTile;
+    static_assert(kTile <= 65536, "tile-local indices fit 16 bits");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -179,14 +198,19 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     // lane j sits at slice + 32k + j, so processing k in order keeps the
     // ranking stable.
     uint64_t key[kItems];
-    uint32_t val[kItems], pos[kItems];
+    uint32_t val[kLean ? 1 : kItems], pos[kItems];
     const uint64_t warp_base = tile_base + (uint64_t)warp * 32 * kItems;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const uint64_t i = warp_base + 32ull * k + lane;
         const bool valid = i < n;
         key[k] = valid ? __ldcs(keys_in + i) : ~0ull;
-        val[k] = valid ? (vals_in ? __ldcs(vals_in + i) : (uint32_t)i) : 0u;
+        if constexpr (kLean) {
+            // One prefetch per 32 values (a 128-byte line) of this item.
+            if (vals_in && lane == 0 && valid) prefetch_l2(vals_in + i);
+        } else {
+            val[k] = valid ? (vals_in ? __ldcs(vals_in + i) : (uint32_t)i) : 0u;
+        }
     }
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
@@ -241,7 +265,10 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
         const uint64_t i = warp_base + 32ull * k + lane;
         if (i < n) {
             sm.u.stage.keys[pos[k]] = key[k];
-            sm.u.stage.vals[pos[k]] = val[k];
+            if constexpr (kLean)
+                sm.u.stage.src[pos[k]] = (uint16_t)(warp * 32u * kItems + 32u * k + lane);
+            else
+                sm.u.stage.vals[pos[k]] = val[k];
         }
     }
     uint32_t prefix = 0;
@@ -252,12 +279,36 @@ __global__ __launch_bounds__(kThreads, kMinBlocks) void sort_pass_kernel(
     sm.global_base[tid] = excl[tid] + prefix;
     __syncthreads();
     const uint32_t tile_n = (uint32_t)min((uint64_t)kTile, (uint64_t)n - tile_base);
-    for (uint32_t i = tid; i < tile_n; i += kThreads) {
-        const uint64_t k = sm.u.stage.keys[i];
-        const uint32_t digit = (uint32_t)(k >> shift) & dmask;
-        const uint32_t o = sm.global_base[digit] + (i - sm.tile_start[digit]);
-        keys_out[o] = k;
-        vals_out[o] = sm.u.stage.vals[i];
+    if constexpr (kLean) {
+        // Gather every value of this thread's slots first (independent
+        // loads in flight), then store.
+        uint32_t v[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t i = tid + (uint32_t)k * kThreads;
+            const uint32_t sidx = i < tile_n ? (uint32_t)sm.u.stage.src[i] : 0u;
+            v[k] = i < tile_n ? (vals_in ? __ldcs(vals_in + tile_base + sidx) : (uint32_t)(tile_base + sidx))
+                              : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t i = tid + (uint32_t)k * kThreads;
+            if (i < tile_n) {
+                const uint64_t key_i = sm.u.stage.keys[i];
+                const uint32_t digit = (uint32_t)(key_i >> shift) & dmask;
+                const uint32_t o = sm.global_base[digit] + (i - sm.tile_start[digit]);
+                keys_out[o] = key_i;
+                vals_out[o] = v[k];
+            }
+        }
+    } else {
+        for (uint32_t i = tid; i < tile_n; i += kThreads) {
+            const uint64_t k = sm.u.stage.keys[i];
+            const uint32_t digit = (uint32_t)(k >> shift) & dmask;
+            const uint32_t o = sm.global_base[digit] + (i - sm.tile_start[digit]);
+            keys_out[o] = k;
+            vals_out[o] = sm.u.stage.vals[i];
+        }
     }
 }
 
@@ -490,6 +541,9 @@ const PassVariant kVariants[] = {
     {8, sort_pass_kernel<8, 4, false>, sizeof(PassSmem<8>), false},
     {12, sort_pass_pipelined_kernel<12, 2>, sizeof(PipeSmem<12>), true},
     {8, sort_pass_pipelined_kernel<8, 3>, sizeof(PipeSmem<8>), true},
+    {12, sort_pass_kernel<12, 4, false, true>, sizeof(PassSmem<12, true>), false},
+    {16, sort_pass_kernel<16, 3, false, true>, sizeof(PassSmem<16, true>), false},
+    {20, sort_pass_kernel<20, 3, true, true>, sizeof(PassSmem<20, true>), false},
 };
 constexpr int kFallbackVariant = 5;  // for inputs a pipelined variant cannot copy
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);

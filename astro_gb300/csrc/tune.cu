@@ -195,7 +195,11 @@ std::vector<uint32_t> Tuner::candidates(Knob knob) const {
         case kBucket: return {8, 16, 32, 64};
         case kGroupSize: return {8, 12, 16, 24, 32, 48, 64};
         case kBlockWarps: return {4, 8};
-        case kSortVariant: return {1, 2, 3, 4, 5, 6, 7, 8, 9};
+        case kSortVariant: {
+            std::vector<uint32_t> v;
+            for (uint32_t i = 1; i <= astro::sort_variant_count(); ++i) v.push_back(i);
+            return v;
+        }
         case kWalkFrontier: return {0, 1};
     }
     return {};

@@ -182,7 +182,10 @@ typedef struct astro_params {
                                  7 = 8/4/ballot; 8 = 12/2 and 9 = 8/3 ballot with
                                  persistent blocks that bulk-copy the next tile
                                  while ranking the current one (16-byte aligned
-                                 inputs; others use 6) */
+                                 inputs; others use 6); lean passes that keep no
+                                 value in registers (values prefetched to L2 and
+                                 gathered by a staged 16-bit index): 10 =
+                                 12/4/ballot, 11 = 16/3/ballot, 12 = 20/3/match */
     uint32_t light_sources;   /* REFERENCE: astro_step runs the lighting pass
                                  with the first light_sources particles (at most
                                  5) as lights (Renderer.swift:539; numStars = 5);

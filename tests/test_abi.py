@@ -131,7 +131,7 @@ def test_argument_errors_without_device(native):
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(group_size=65)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
-    bad = p.replace(sort_variant=10)
+    bad = p.replace(sort_variant=13)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1
     bad = p.replace(open_delta_weight=-1.0)
     assert lib().astro_create(byref(bad), 100, 1, byref(h)) == -1

@@ -198,7 +198,8 @@ def test_physical_fast_within_tolerance(ag, oracle, walk, warps, persistent):
 
 @pytest.mark.parametrize("group_size,sort_variant,form", [(8, 1, 0), (16, 4, 1), (1, 7, 0),
                                                          (32, 6, 1), (5, 2, 0), (24, 3, 0),
-                                                         (12, 5, 0), (32, 8, 0), (20, 9, 1)])
+                                                         (12, 5, 0), (32, 8, 0), (20, 9, 1),
+                                                         (16, 10, 0), (48, 11, 1), (64, 12, 0)])
 def test_group_size_and_sort_variant_bit_exact(ag, oracle, group_size, sort_variant, form):
     """Particles per warp and the sort's pass kernel are tuning knobs: every
     setting must give the oracle's tree and accelerations bit for bit."""
@@ -517,11 +518,12 @@ print("ok")
 """
 
 
-@pytest.mark.parametrize("variant_index", [7, 8])
-def test_pipelined_sort_variants_match_stable_argsort(ag, tmp_path, variant_index):
-    """The pipelined pass kernels (sort_variant 8 and 9, selected here as the
-    library default through ASTRO_SORT_VARIANT in a fresh process): whole and
-    partial tiles, given indices, and unaligned inputs that fall back."""
+@pytest.mark.parametrize("variant_index", [7, 8, 9, 10, 11])
+def test_sort_variants_match_stable_argsort(ag, tmp_path, variant_index):
+    """The pipelined pass kernels (sort_variant 8 and 9) and the lean ones
+    (10 to 12), each selected as the library default through
+    ASTRO_SORT_VARIANT in a fresh process: whole and partial tiles, given
+    indices, and unaligned inputs (the pipelined kernels fall back)."""
     import os
     import subprocess
     import sys

@@ -28,7 +28,7 @@ def test_autotune_candidates_stay_in_range():
         assert c == sorted(c) and all(3 <= v <= 21 for v in c)
     assert autotune.candidates("group_size", 1000)[-1] == 64  # two particles per lane
     assert set(autotune.candidates("block_warps", 1)) <= {2, 4, 8}
-    assert autotune.candidates("sort_variant", 1) == list(range(1, 10))
+    assert autotune.candidates("sort_variant", 1) == list(range(1, 13))
     assert all(0 < w < 1 for w in autotune.candidates("open_delta_weight", 1))
     assert all(0 < r <= 0.5 for r in autotune.candidates("far_ratio", 1))
     assert set(autotune.ACCURACY_KNOBS) <= set(autotune.KNOBS)
