@@ -588,6 +588,17 @@ int settle_traverse(astro_ctx* ctx) {
 
 }  // namespace
 
+// Steps launched since the last device check are checked (and rerun after
+// a group-walk overflow) before any call that reads or replaces the state,
+// so no call sees a state whose steps may still be run again.
+#define SETTLE()                                                        \
+    do {                                                                \
+        if (ctx && ctx->pending_steps > 0) {                            \
+            const int settle_r_ = check_device(ctx);                    \
+            if (settle_r_ != ASTRO_OK) return settle_r_;                \
+        }                                                               \
+    } while (0)
+
 // ------------------------------------------------------------------ ABI --
 
 extern "C" {
@@ -787,6 +798,7 @@ int astro_get_params(const astro_ctx* ctx, astro_params* out) {
 // Changing preset, form or lbits discards the uploaded state (upload again);
 // the other fields take effect at the next step.
 int astro_set_params(astro_ctx* ctx, const astro_params* params) {
+    SETTLE();
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     const char* why = nullptr;
     int r = validate_params(params, &why);
@@ -915,6 +927,7 @@ static int upload_particles(astro_ctx* ctx, const PositionMass* pm, const Veloci
 
 int astro_upload(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
                  const ColorType* ct, uint32_t n, uint32_t n_tree) {
+    SETTLE();
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     if (!pm || !vr || n == 0 || n_tree > n)
         return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload: null pointer, n == 0 or n_tree > n");
@@ -927,6 +940,7 @@ int astro_upload(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* v
 
 int astro_upload_systems(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
                          const uint32_t* sys_sizes, uint32_t nsys) {
+    SETTLE();
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     if (!pm || !vr || !sys_sizes || nsys == 0)
         return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload_systems: null pointer or nsys == 0");
@@ -943,6 +957,7 @@ int astro_upload_systems(astro_ctx* ctx, const PositionMass* pm, const VelocityR
 }
 
 int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n) {
+    SETTLE();
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     if (!ctx->uploaded) return fail(ctx, ASTRO_ERR_STATE, "download before upload");
     if (n != ctx->n || (!pm && !vr)) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "download: n mismatch");
@@ -964,16 +979,19 @@ int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_
     } while (0)
 
 int astro_encode(astro_ctx* ctx) {
+    SETTLE();
     NEED_UPLOAD();
     drop_graph(ctx);
     return stage_encode(ctx);
 }
 int astro_sort(astro_ctx* ctx) {
+    SETTLE();
     NEED_UPLOAD();
     drop_graph(ctx);
     return stage_sort(ctx);
 }
 int astro_build(astro_ctx* ctx) {
+    SETTLE();
     NEED_UPLOAD();
     drop_graph(ctx);
     return stage_build(ctx);
@@ -987,6 +1005,7 @@ int astro_traverse(astro_ctx* ctx) {
     return group_walk(ctx) ? settle_traverse(ctx) : ASTRO_OK;
 }
 int astro_integrate(astro_ctx* ctx, float dt) {
+    SETTLE();
     NEED_UPLOAD();
     drop_graph(ctx);
     return stage_integrate(ctx, dt);
@@ -1016,6 +1035,7 @@ int astro_get_stream(astro_ctx* ctx, void** stream) {
 
 int astro_read_keys(astro_ctx* ctx, uint64_t* codes, uint64_t* sorted_codes,
                     uint32_t* sorted_indices, uint32_t n) {
+    SETTLE();
     NEED_UPLOAD();
     const uint32_t count = is_phys(ctx) ? ctx->n : ctx->n_tree;
     if (n != count) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_keys: n must be the tree count");
@@ -1041,6 +1061,7 @@ int astro_read_keys(astro_ctx* ctx, uint64_t* codes, uint64_t* sorted_codes,
 
 int astro_read_tree_info(astro_ctx* ctx, uint32_t* n_layers, uint32_t* layer_sizes,
                          uint32_t* layer_offsets, uint32_t* layer_counts, uint32_t max_layers) {
+    SETTLE();
     NEED_UPLOAD();
     const uint32_t L = ctx->layers.n_layers;
     if (n_layers) *n_layers = L;
@@ -1058,6 +1079,7 @@ int astro_read_tree_info(astro_ctx* ctx, uint32_t* n_layers, uint32_t* layer_siz
 }
 
 int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t count) {
+    SETTLE();
     NEED_UPLOAD();
     if (!nodes || first + count > ctx->capacity)
         return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_nodes: range outside the node capacity");
@@ -1089,6 +1111,7 @@ int astro_read_nodes(astro_ctx* ctx, OctreeNode* nodes, uint64_t first, uint64_t
 }
 
 int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n) {
+    SETTLE();
     NEED_UPLOAD();
     if (!acc4 || n != ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_accel: n mismatch");
     cudaStream_t st = ctx->stream;
@@ -1104,6 +1127,7 @@ int astro_read_accel(astro_ctx* ctx, float* acc4, uint32_t n) {
 
 int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visits,
                      uint64_t* cell_interactions) {
+    SETTLE();
     NEED_UPLOAD();
     unsigned long long s[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(s, ctx->stats, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1115,6 +1139,7 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
 }
 
 int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions) {
+    SETTLE();
     NEED_UPLOAD();
     unsigned long long s[kNumStats] = {0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(s, ctx->stats, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1125,6 +1150,7 @@ int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_inte
 }
 
 int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms) {
+    SETTLE();
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     if (!ctx->trav_timed) return fail(ctx, ASTRO_ERR_STATE, "no timed group walk stage call yet");
     CK(cudaEventSynchronize(ctx->trav_ev[2]));
@@ -1138,6 +1164,7 @@ int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms) {
 
 int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t n_sample,
                            double* acc3) {
+    SETTLE();
     NEED_UPLOAD();
     if (!sample_idx || !acc3 || n_sample == 0 || n_sample > ctx->n)
         return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "direct_accel: bad samples");
@@ -1184,6 +1211,7 @@ int astro_direct_accel_f64(astro_ctx* ctx, const uint32_t* sample_idx, uint32_t 
 }
 
 int astro_lighting(astro_ctx* ctx, uint32_t num_stars) {
+    SETTLE();
     NEED_UPLOAD();
     if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "lighting needs the REFERENCE preset");
     CK(astro::launch_lighting(ctx->pos[0], ctx->types, ctx->colors, ctx->lights, ctx->n, num_stars,
@@ -1192,6 +1220,7 @@ int astro_lighting(astro_ctx* ctx, uint32_t num_stars) {
 }
 
 int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n) {
+    SETTLE();
     NEED_UPLOAD();
     if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "colours need the REFERENCE preset");
     if (!ct || n != ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "read_colors: n mismatch");
@@ -1203,6 +1232,7 @@ int astro_read_colors(astro_ctx* ctx, ColorType* ct, uint32_t n) {
 
 int astro_splat(astro_ctx* ctx, const astro_camera* camera, uint32_t width, uint32_t height,
                 const float* clear, float* rgba, float* depth) {
+    SETTLE();
     NEED_UPLOAD();
     if (is_phys(ctx)) return fail(ctx, ASTRO_ERR_NOT_SUPPORTED, "the splat draws the REFERENCE preset");
     if (!camera || !rgba || width == 0 || height == 0)
@@ -1300,6 +1330,7 @@ struct File {
 extern "C" {
 
 int astro_save_state(astro_ctx* ctx, const char* path, uint64_t step, double time) {
+    SETTLE();
     NEED_UPLOAD();
     if (!path) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "save_state: path is NULL");
     if (ctx->state_in_b) return fail(ctx, ASTRO_ERR_STATE, "save_state in the middle of a step");

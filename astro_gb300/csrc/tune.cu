@@ -334,6 +334,9 @@ extern "C" int astro_autotune_keep(astro_ctx* ctx, const char* path, float targe
         ctx->last_error = "autotune: no particles uploaded";
         return ASTRO_ERR_STATE;
     }
+    // Steps still unchecked finish (and rerun if their walk overflowed)
+    // before the tuner reads the particles.
+    if (int r = astro_synchronize(ctx); r != ASTRO_OK) return r;
     if (ctx->p.preset != ASTRO_PRESET_PHYSICAL) {
         ctx->last_error = "autotune: the REFERENCE preset's knobs are the reference's constants";
         return ASTRO_ERR_NOT_SUPPORTED;

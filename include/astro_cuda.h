@@ -301,8 +301,12 @@ int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms);
  * and particles as they were, and at the next check of the device
  * (astro_synchronize, a readback) the buffers grow to the counted need and
  * the skipped steps run again, so the results equal those of buffers large
- * enough from the start. Stage calls (astro_traverse) do the same before
- * returning. Reports the pool size in blocks, the frontier buffer size in
+ * enough from the start. Every call that reads or replaces the state
+ * (readbacks, uploads, stage calls, parameter changes, saving) first waits
+ * for the steps launched since the last check, so none sees a state whose
+ * steps may still run again; astro_step and astro_step_batched themselves
+ * do not wait. Stage calls (astro_traverse) rerun their own traversal
+ * before returning. Reports the pool size in blocks, the frontier buffer size in
  * words and the steps and traversals run again since astro_create (any
  * pointer may be NULL). Waits for the context's stream. */
 int astro_read_walk_buffers(astro_ctx* ctx, uint64_t* list_blocks, uint32_t* frontier_cap,

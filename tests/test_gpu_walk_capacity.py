@@ -43,7 +43,7 @@ def _case(ag, form, batched, no_graph):
     return p, pm, vr, None
 
 
-def _run(ag, p, pm, vr, sizes, steps, blocks=0, frontier=0):
+def _run(ag, p, pm, vr, sizes, steps, blocks=0, frontier=0, sync=True):
     with ag.Simulation(p, max_n=len(pm), max_systems=len(sizes) if sizes else 1) as sim:
         if sizes:
             sim.upload_systems(pm, vr, sizes)
@@ -52,10 +52,24 @@ def _run(ag, p, pm, vr, sizes, steps, blocks=0, frontier=0):
         if blocks or frontier:
             _capacity(sim, blocks, frontier)
         sim.draw(5e-4, steps)
-        sim.synchronize()
+        if sync:
+            sim.synchronize()
         out = dict(state=sim.download(), acc=sim.read_accel(), stats=sim.read_stats(),
                    far=sim.read_far_stats(), capacity=_capacity(sim))
     return out
+
+
+def test_readbacks_wait_for_the_rerun(native):
+    """A readback right after the steps (no explicit synchronize) sees the
+    state of the rerun steps, not the state the skipped evaluations left."""
+    ag = native
+    L = ag.layouts
+    p, pm, vr, sizes = _case(ag, L.FORM_PLAIN, False, False)
+    want = _run(ag, p, pm.copy(), vr.copy(), sizes, 2)
+    got = _run(ag, p, pm.copy(), vr.copy(), sizes, 2, 1, 2, sync=False)
+    for a, b in zip(got["state"], want["state"]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(got["acc"], want["acc"]) and got["capacity"][2] >= 2
 
 
 @pytest.mark.parametrize("form,batched,no_graph,blocks,frontier", [
