@@ -86,6 +86,8 @@ SIGNATURES = {
     "astro_test_sort_lookback_timeout": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32,
                                                  c_uint32, c_uint32, c_void_p, c_size_t,
                                                  c_void_p]),
+    "astro_upload_async": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32]),
+    "astro_download_async": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32]),
     "astro_test_walk_capacity": (c_int, [c_void_p, c_uint64, c_uint32]),
     "astro_read_walk_buffers": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "astro_generate_ic": (c_int, [c_uint32, c_uint64, c_uint32, c_uint32, c_double, c_double,

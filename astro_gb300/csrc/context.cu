@@ -192,6 +192,7 @@ int grow_walk_buffers(astro_ctx* ctx, uint32_t* evals_done) {
         ctx->frontier_cap = (uint32_t)((want + 3) & ~3ull);
     }
     ctx->lists_blocks_want = std::min<size_t>(ctx->lists_blocks_want, 0xFFFFFF00ull);
+    drop_graph(ctx);  // the captured step holds the old buffers and sizes
     CK(cudaMemset(ctx->counters + 4, 0, sizeof(c)));
     CK(cudaMemset(ctx->err, 0, sizeof(uint32_t)));
     return ensure_frontier(ctx);
@@ -202,8 +203,23 @@ int grow_walk_buffers(astro_ctx* ctx, uint32_t* evals_done) {
 // larger buffers, so the state continues exactly as without the overflow.
 int check_device(astro_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h2d_stream) CK(cudaStreamSynchronize(ctx->h2d_stream));
+    if (ctx->d2h_stream) CK(cudaStreamSynchronize(ctx->d2h_stream));
     uint32_t err = 0;
     CK(cudaMemcpy(&err, ctx->err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err == astro::kErrFrontier && ctx->pending_steps > 0 && ctx->steps_unrerunnable) {
+        // Asynchronous transfers replaced or delivered the state of steps
+        // that were skipped: they cannot be run again here.
+        uint32_t done = 0;
+        int r = grow_walk_buffers(ctx, &done);
+        ctx->pending_steps = 0;
+        ctx->steps_unrerunnable = false;
+        if (r != ASTRO_OK) return r;
+        return fail(ctx, ASTRO_ERR_DEVICE_OVERFLOW,
+                    "a group walk outgrew its buffers during steps whose state asynchronous "
+                    "transfers replaced or read; the buffers have grown: run those steps again");
+    }
+    ctx->steps_unrerunnable = false;
     for (int attempt = 0; err == astro::kErrFrontier && ctx->pending_steps > 0 && attempt < 16;
          ++attempt) {
         uint32_t done = 0;
@@ -268,6 +284,7 @@ int ensure_frontier(astro_ctx* ctx) {
     if (!group_walk(ctx)) return ASTRO_OK;
     const size_t words = (size_t)astro::group_walk_warps() * 2 * ctx->frontier_cap;
     if (words > ctx->frontier_words) {
+        drop_graph(ctx);  // a captured step holds the old buffers
         dev_free(ctx->frontier);
         ctx->frontier_words = 0;
         CK(dev_alloc(&ctx->frontier, words));
@@ -280,6 +297,7 @@ int ensure_frontier(astro_ctx* ctx) {
                                                                      : astro::kDefaultGroupSize);
     const size_t blocks = std::max(estimate, ctx->lists_blocks_want);
     if (blocks > ctx->lists_blocks) {
+        drop_graph(ctx);
         dev_free(ctx->lists);
         dev_free(ctx->list_next);
         ctx->lists_blocks = 0;
@@ -558,7 +576,9 @@ int launch_steps(astro_ctx* ctx, float dt, uint32_t nsteps) {
             if ((r = run_step(ctx, dt)) != ASTRO_OK) return r;
         return ASTRO_OK;
     }
-    // The step is captured once per (upload, params, dt) and replayed.
+    // Walk buffers are sized outside the capture (no allocation inside it);
+    // the step is captured once per (upload, params, dt) and replayed.
+    if ((r = ensure_frontier(ctx)) != ASTRO_OK) return r;
     if (!(ctx->graph_valid && ctx->graph_dt == dt))
         if ((r = capture_step(ctx, dt)) != ASTRO_OK) return r;
     for (uint32_t s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
@@ -730,6 +750,8 @@ int astro_create(const astro_params* params, uint32_t max_n, uint32_t max_system
 int astro_destroy(astro_ctx* ctx) {
     if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->h2d_stream) cudaStreamSynchronize(ctx->h2d_stream);
+    if (ctx->d2h_stream) cudaStreamSynchronize(ctx->d2h_stream);
     drop_graph(ctx);
     for (int b = 0; b < 2; ++b) {
         dev_free(ctx->pos[b]);
@@ -753,6 +775,15 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->sorted_keys);
     dev_free(ctx->perm);
     if (ctx->staging) cudaFree(ctx->staging);
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->stage_in[i]) cudaFree(ctx->stage_in[i]);
+        if (ctx->stage_out[i]) cudaFree(ctx->stage_out[i]);
+        for (cudaEvent_t e : {ctx->ev_in_copied[i], ctx->ev_in_used[i], ctx->ev_out_ready[i],
+                              ctx->ev_out_copied[i]})
+            if (e) cudaEventDestroy(e);
+    }
+    if (ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
+    if (ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
     if (ctx->sort_temp) cudaFree(ctx->sort_temp);
     dev_free(ctx->topo_lookback);
     dev_free(ctx->counters);
@@ -895,6 +926,22 @@ static int upload_common(astro_ctx* ctx, const PositionMass* pm, const VelocityR
     return upload_particles(ctx, pm, vr, ct, n, n_tree);
 }
 
+// Copy streams, staging slots and events of the asynchronous transfers.
+static int ensure_async(astro_ctx* ctx) {
+    if (ctx->d2h_stream) return ASTRO_OK;
+    const size_t bytes = 64ull * ctx->max_n;
+    for (int i = 0; i < 2; ++i) {
+        if (!ctx->stage_in[i]) CK(cudaMalloc(&ctx->stage_in[i], bytes));
+        if (!ctx->stage_out[i]) CK(cudaMalloc(&ctx->stage_out[i], bytes));
+        for (cudaEvent_t* e : {&ctx->ev_in_copied[i], &ctx->ev_in_used[i], &ctx->ev_out_ready[i],
+                               &ctx->ev_out_copied[i]})
+            if (!*e) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    if (!ctx->h2d_stream) CK(cudaStreamCreateWithFlags(&ctx->h2d_stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking));
+    return ASTRO_OK;
+}
+
 // The particle copy of an upload: host arrays through the staging buffer into
 // the state (A) buffers, ids 0..n-1, types and colours.
 static int upload_particles(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
@@ -970,6 +1017,67 @@ int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_
     if (pm) CK(cudaMemcpyAsync(pm, d_pm, sizeof(PositionMass) * n, cudaMemcpyDeviceToHost, st));
     if (vr) CK(cudaMemcpyAsync(vr, d_vr, sizeof(VelocityRadius) * n, cudaMemcpyDeviceToHost, st));
     return check_device(ctx);
+}
+
+int astro_upload_async(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                       uint32_t n) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!pm || !vr) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload_async: null pointer");
+    if (!ctx->uploaded)
+        return fail(ctx, ASTRO_ERR_STATE, "upload_async: needs an earlier upload (it keeps that layout)");
+    if (n != ctx->n) return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "upload_async: n differs from the upload's");
+    int r = ensure_async(ctx);
+    if (r != ASTRO_OK) return r;
+    if (ctx->pending_steps > 0) ctx->steps_unrerunnable = true;
+    const uint32_t s = ctx->in_slot;
+    ctx->in_slot ^= 1u;
+    char* stg = static_cast<char*>(ctx->stage_in[s]);
+    PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
+    VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);
+    // The slot is free once the conversion that last read it has run; the
+    // copy itself overlaps the steps queued before it.
+    CK(cudaStreamWaitEvent(ctx->h2d_stream, ctx->ev_in_used[s], 0));
+    CK(cudaMemcpyAsync(d_pm, pm, sizeof(PositionMass) * n, cudaMemcpyHostToDevice, ctx->h2d_stream));
+    CK(cudaMemcpyAsync(d_vr, vr, sizeof(VelocityRadius) * n, cudaMemcpyHostToDevice, ctx->h2d_stream));
+    CK(cudaEventRecord(ctx->ev_in_copied[s], ctx->h2d_stream));
+    // The state is replaced in step-stream order, after the queued steps;
+    // particle types and colours stay those of the last upload.
+    cudaStream_t st = ctx->stream;
+    CK(cudaStreamWaitEvent(st, ctx->ev_in_copied[s], 0));
+    CK(astro::launch_upload_convert(is_prec(ctx), d_pm, d_vr, nullptr, ctx->pos[0], ctx->vel[0],
+                                    is_phys(ctx) ? ctx->ids[0] : nullptr, nullptr, ctx->x64[0], n,
+                                    ctx->n_tree, st));
+    CK(cudaEventRecord(ctx->ev_in_used[s], st));
+    ctx->tree_valid = false;
+    ctx->state_in_b = false;
+    return ASTRO_OK;
+}
+
+int astro_download_async(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n) {
+    if (!ctx) return ASTRO_ERR_INVALID_ARGUMENT;
+    if (!ctx->uploaded) return fail(ctx, ASTRO_ERR_STATE, "download before upload");
+    if (n != ctx->n || (!pm && !vr))
+        return fail(ctx, ASTRO_ERR_INVALID_ARGUMENT, "download_async: n mismatch or no output");
+    int r = ensure_async(ctx);
+    if (r != ASTRO_OK) return r;
+    if (ctx->pending_steps > 0) ctx->steps_unrerunnable = true;
+    const uint32_t s = ctx->out_slot;
+    ctx->out_slot ^= 1u;
+    char* stg = static_cast<char*>(ctx->stage_out[s]);
+    PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
+    VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);
+    cudaStream_t st = ctx->stream;
+    // The slot is free once its last copy to the host has run; the copy of
+    // this state overlaps the steps queued after it.
+    CK(cudaStreamWaitEvent(st, ctx->ev_out_copied[s], 0));
+    const Cur c = current(ctx);
+    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st));
+    CK(cudaEventRecord(ctx->ev_out_ready[s], st));
+    CK(cudaStreamWaitEvent(ctx->d2h_stream, ctx->ev_out_ready[s], 0));
+    if (pm) CK(cudaMemcpyAsync(pm, d_pm, sizeof(PositionMass) * n, cudaMemcpyDeviceToHost, ctx->d2h_stream));
+    if (vr) CK(cudaMemcpyAsync(vr, d_vr, sizeof(VelocityRadius) * n, cudaMemcpyDeviceToHost, ctx->d2h_stream));
+    CK(cudaEventRecord(ctx->ev_out_copied[s], ctx->d2h_stream));
+    return ASTRO_OK;
 }
 
 #define NEED_UPLOAD()                                                          \

@@ -122,6 +122,19 @@ struct astro_ctx {
     uint32_t* perm = nullptr;
     void* staging = nullptr;          // upload/download, 64 B per particle
     size_t staging_bytes = 0;
+    // Asynchronous upload/download (created on first use): a copy stream
+    // each way, two staging slots each way (64 B per particle each), and the
+    // events that order copies, conversions and the step stream.
+    cudaStream_t h2d_stream = nullptr;
+    cudaStream_t d2h_stream = nullptr;
+    void* stage_in[2] = {nullptr, nullptr};
+    void* stage_out[2] = {nullptr, nullptr};
+    cudaEvent_t ev_in_copied[2] = {nullptr, nullptr};   // host -> slot copy done
+    cudaEvent_t ev_in_used[2] = {nullptr, nullptr};     // slot converted into the state
+    cudaEvent_t ev_out_ready[2] = {nullptr, nullptr};   // state converted into the slot
+    cudaEvent_t ev_out_copied[2] = {nullptr, nullptr};  // slot -> host copy done
+    uint32_t in_slot = 0, out_slot = 0;
+    bool steps_unrerunnable = false;  // an async transfer touched the state of unchecked steps
 
     // Tree.
     uint64_t tree_capacity = 0;       // allocated node slots

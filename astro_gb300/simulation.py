@@ -37,6 +37,7 @@ class Simulation:
         self.n = 0
         self.n_tree = 0
         self.sys_sizes: list[int] = []
+        self._async_refs: list = []  # host arrays of queued asynchronous transfers
 
     # -- lifetime ---------------------------------------------------------
     def close(self) -> None:
@@ -87,6 +88,27 @@ class Simulation:
         self.n = self.n_tree = int(sz.sum())
         self.sys_sizes = [int(s) for s in sz]
 
+    def upload_async(self, pm: np.ndarray, vr: np.ndarray) -> None:
+        """Replace the particles with len(pm) new ones in the last upload's
+        layout, without waiting: the copy overlaps the steps queued before
+        it. The arrays (pinned memory for the overlap) are kept alive until
+        synchronize()."""
+        if pm.dtype != L.POSITION_MASS or vr.dtype != L.VELOCITY_RADIUS or \
+                not (pm.flags.c_contiguous and vr.flags.c_contiguous):
+            raise TypeError("upload_async needs contiguous POSITION_MASS / VELOCITY_RADIUS arrays")
+        self._check(lib().astro_upload_async(self._h, ptr(pm), ptr(vr), len(pm)))
+        self._async_refs.extend((pm, vr))
+
+    def download_async(self, pm: np.ndarray, vr: np.ndarray) -> None:
+        """Queue a copy of the state (as after the steps queued so far) into
+        pm and vr without waiting; they hold it once synchronize() returns."""
+        if pm.dtype != L.POSITION_MASS or vr.dtype != L.VELOCITY_RADIUS or \
+                not (pm.flags.c_contiguous and vr.flags.c_contiguous) or not pm.flags.writeable:
+            raise TypeError("download_async needs writable contiguous POSITION_MASS / "
+                            "VELOCITY_RADIUS arrays")
+        self._check(lib().astro_download_async(self._h, ptr(pm), ptr(vr), self.n))
+        self._async_refs.extend((pm, vr))
+
     def download(self, pm: np.ndarray | None = None, vr: np.ndarray | None = None):
         pm = np.zeros(self.n, L.POSITION_MASS) if pm is None else pm
         vr = np.zeros(self.n, L.VELOCITY_RADIUS) if vr is None else vr
@@ -114,6 +136,7 @@ class Simulation:
         sim.max_n = max(max_n, hdr.n)
         sim.n, sim.n_tree = hdr.n, hdr.n_tree
         sim.sys_sizes = [int(s) for s in sizes]
+        sim._async_refs = []
         return sim, step.value, t.value
 
     # -- stages (Renderer.draw order) -------------------------------------
@@ -191,7 +214,10 @@ class Simulation:
         return out
 
     def synchronize(self) -> None:
-        self._check(lib().astro_synchronize(self._h))
+        try:
+            self._check(lib().astro_synchronize(self._h))
+        finally:
+            self._async_refs.clear()
 
     @property
     def stream(self) -> int:

@@ -241,6 +241,26 @@ int astro_upload_systems(astro_ctx* ctx, const PositionMass* pm, const VelocityR
 /* Copy the particle state back (waits for the stream). */
 int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n);
 
+/* Pipelined transfers for a stream of independent inputs: neither call
+ * waits. astro_upload_async replaces the state with n new particles in the
+ * layout of the last astro_upload / astro_upload_systems (same n, same
+ * systems, the same particle types and colours in the REFERENCE preset),
+ * taking effect in stream order after the steps already queued;
+ * its host-to-device copy runs on a copy stream of its own, so it overlaps
+ * those steps. astro_download_async delivers the state as it is after the
+ * steps queued before it; its device-to-host copy also runs on its own
+ * stream and overlaps the steps queued after it. Two staging slots each way
+ * let one transfer per direction be in flight while the next is queued.
+ * The host buffers must stay valid, and the downloaded ones unread, until
+ * astro_synchronize returns; pinned (page-locked) host memory is needed for
+ * the copies to overlap. If a group walk outgrew its buffers during steps
+ * whose state such a transfer replaced or read, those steps cannot be run
+ * again: the next astro_synchronize grows the buffers and returns
+ * ASTRO_ERR_DEVICE_OVERFLOW, and the batch should be run again. */
+int astro_upload_async(astro_ctx* ctx, const PositionMass* pm, const VelocityRadius* vr,
+                       uint32_t n);
+int astro_download_async(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_t n);
+
 /* Stage calls, in step order. Each is stream-ordered and does not wait. */
 int astro_encode(astro_ctx* ctx);    /* generateMortonCodes + fillIndices (MortonCode.metal:26-52, Octree.metal:39-51) */
 int astro_sort(astro_ctx* ctx);      /* radixSorter.sort at layer 0 (Renderer.swift:522-528) */
