@@ -900,6 +900,28 @@ __global__ void download_convert_kernel(const float4* __restrict__ pos, const fl
     *reinterpret_cast<float4*>(&vr[i].radius) = make_float4(v.w, 0.f, 0.f, 0.f);
 }
 
+// The same conversion as a gather: output slot o (upload order) reads state
+// slot inv[o] (inv = the inverse of ids), so the 64 bytes written per
+// particle are contiguous across a warp and only the reads are scattered.
+template <bool kPrec>
+__global__ void download_gather_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                       const uint32_t* __restrict__ inv,
+                                       const double* __restrict__ x64, PositionMass* __restrict__ pm,
+                                       VelocityRadius* __restrict__ vr, uint32_t n) {
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const uint32_t j = inv ? __ldg(&inv[o]) : o;
+    const float4 p = __ldg(&pos[j]), v = __ldg(&vel[j]);
+    float4 out_p = make_float4(p.x, p.y, p.z, 0.f);
+    if (kPrec)
+        out_p = make_float4(__double2float_rn(x64[j]), __double2float_rn(x64[(size_t)n + j]),
+                            __double2float_rn(x64[2 * (size_t)n + j]), 0.f);
+    *reinterpret_cast<float4*>(&pm[o].position[0]) = out_p;
+    *reinterpret_cast<float4*>(&pm[o].mass) = make_float4(p.w, 0.f, 0.f, 0.f);
+    *reinterpret_cast<float4*>(&vr[o].velocity[0]) = make_float4(v.x, v.y, v.z, 0.f);
+    *reinterpret_cast<float4*>(&vr[o].radius) = make_float4(v.w, 0.f, 0.f, 0.f);
+}
+
 // Scatter a per-state-slot array back to upload order through ids.
 template <typename T>
 __global__ void scatter_by_id_kernel(const T* __restrict__ src, const uint32_t* __restrict__ ids,
@@ -1236,7 +1258,21 @@ cudaError_t launch_upload_convert(bool prec, const PositionMass* pm, const Veloc
 
 cudaError_t launch_download_convert(bool prec, const float4* pos, const float4* vel,
                                     const uint32_t* ids, const double* x64, PositionMass* pm,
-                                    VelocityRadius* vr, uint32_t n, cudaStream_t st) {
+                                    VelocityRadius* vr, uint32_t n, cudaStream_t st,
+                                    uint32_t* inv_scratch) {
+    if (inv_scratch || !ids) {
+        // The inverse permutation (a 4-byte scatter), then a gather with
+        // contiguous 64-byte writes.
+        if (ids) inverse_ids_kernel<<<blocks_for(n, 256), 256, 0, st>>>(ids, inv_scratch, n);
+        const uint32_t* inv = ids ? inv_scratch : nullptr;
+        if (prec)
+            download_gather_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, inv, x64, pm,
+                                                                             vr, n);
+        else
+            download_gather_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, inv, x64, pm,
+                                                                              vr, n);
+        return cudaGetLastError();
+    }
     if (prec)
         download_convert_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(pos, vel, ids, x64, pm,
                                                                           vr, n);

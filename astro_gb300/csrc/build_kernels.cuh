@@ -180,9 +180,12 @@ cudaError_t launch_upload_convert(bool prec, const PositionMass* pm, const Veloc
                                   const ColorType* ct, float4* pos, float4* vel, uint32_t* ids,
                                   uint32_t* types, double* x64, uint32_t n, uint32_t n_tree,
                                   cudaStream_t st);
+// With inv_scratch (n words) the state is gathered into upload order
+// through the inverse of ids; without, scattered through ids.
 cudaError_t launch_download_convert(bool prec, const float4* pos, const float4* vel,
                                     const uint32_t* ids, const double* x64, PositionMass* pm,
-                                    VelocityRadius* vr, uint32_t n, cudaStream_t st);
+                                    VelocityRadius* vr, uint32_t n, cudaStream_t st,
+                                    uint32_t* inv_scratch = nullptr);
 cudaError_t launch_scatter_u64(const uint64_t* src, const uint32_t* ids, uint64_t* dst, uint32_t n,
                                cudaStream_t st);
 cudaError_t launch_scatter_f4(const float4* src, const uint32_t* ids, float4* dst, uint32_t n,

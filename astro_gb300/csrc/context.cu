@@ -775,6 +775,7 @@ int astro_destroy(astro_ctx* ctx) {
     dev_free(ctx->sorted_keys);
     dev_free(ctx->perm);
     if (ctx->staging) cudaFree(ctx->staging);
+    dev_free(ctx->dl_inv);
     for (int i = 0; i < 2; ++i) {
         if (ctx->stage_in[i]) cudaFree(ctx->stage_in[i]);
         if (ctx->stage_out[i]) cudaFree(ctx->stage_out[i]);
@@ -1013,7 +1014,9 @@ int astro_download(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, uint32_
     char* stg = static_cast<char*>(ctx->staging);
     PositionMass* d_pm = reinterpret_cast<PositionMass*>(stg);
     VelocityRadius* d_vr = reinterpret_cast<VelocityRadius*>(stg + 32ull * ctx->max_n);
-    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st));
+    if (c.ids && !ctx->dl_inv) CK(dev_alloc(&ctx->dl_inv, ctx->max_n));
+    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st,
+                                      ctx->dl_inv));
     if (pm) CK(cudaMemcpyAsync(pm, d_pm, sizeof(PositionMass) * n, cudaMemcpyDeviceToHost, st));
     if (vr) CK(cudaMemcpyAsync(vr, d_vr, sizeof(VelocityRadius) * n, cudaMemcpyDeviceToHost, st));
     return check_device(ctx);
@@ -1071,7 +1074,9 @@ int astro_download_async(astro_ctx* ctx, PositionMass* pm, VelocityRadius* vr, u
     // this state overlaps the steps queued after it.
     CK(cudaStreamWaitEvent(st, ctx->ev_out_copied[s], 0));
     const Cur c = current(ctx);
-    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st));
+    if (c.ids && !ctx->dl_inv) CK(dev_alloc(&ctx->dl_inv, ctx->max_n));
+    CK(astro::launch_download_convert(is_prec(ctx), c.pos, c.vel, c.ids, c.x64, d_pm, d_vr, n, st,
+                                      ctx->dl_inv));
     CK(cudaEventRecord(ctx->ev_out_ready[s], st));
     CK(cudaStreamWaitEvent(ctx->d2h_stream, ctx->ev_out_ready[s], 0));
     if (pm) CK(cudaMemcpyAsync(pm, d_pm, sizeof(PositionMass) * n, cudaMemcpyDeviceToHost, ctx->d2h_stream));

@@ -134,6 +134,7 @@ struct astro_ctx {
     cudaEvent_t ev_out_ready[2] = {nullptr, nullptr};   // state converted into the slot
     cudaEvent_t ev_out_copied[2] = {nullptr, nullptr};  // slot -> host copy done
     uint32_t in_slot = 0, out_slot = 0;
+    uint32_t* dl_inv = nullptr;       // downloads: inverse of the ids (upload order -> slot)
     bool steps_unrerunnable = false;  // an async transfer touched the state of unchecked steps
 
     // Tree.
