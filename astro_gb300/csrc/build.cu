@@ -409,6 +409,22 @@ __device__ __forceinline__ uint32_t reserve_groups(uint32_t* counter, uint32_t c
     return __shfl_sync(mask, base, leader) + prefix;
 }
 
+// Visits the particles [pb, pe) in order, loading four at a time so that
+// four loads are in flight (the sums stay in particle order).
+template <typename F>
+__device__ __forceinline__ void for_particles(const float4* __restrict__ pos, uint32_t pb,
+                                              uint32_t pe, F&& f) {
+    uint32_t i = pb;
+    for (; i + 4u <= pe; i += 4u) {
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = __ldg(&pos[i + u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) f(q[u]);
+    }
+    for (; i < pe; ++i) f(__ldg(&pos[i]));
+}
+
 // Mass moments of a leaf's particles about a point c (the cell's centre):
 // first moments D = sum m d and second moments S = sum m d d^T, d = x - c,
 // in FP32, each product and sum rounded separately. quadrupole() shifts them
@@ -507,14 +523,13 @@ __device__ __forceinline__ void aggregate_leaf_node_q(const AggArgs& a, uint32_t
         }
     } else if (kMode == 1) {
         float m = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
-        for (uint32_t i = pb; i < pe; ++i) {
-            const float4 q = a.pos[i];
+        for_particles(a.pos, pb, pe, [&](const float4 q) {
             m = __fadd_rn(m, q.w);
             sx = __fadd_rn(sx, __fmul_rn(q.w, q.x));
             sy = __fadd_rn(sy, __fmul_rn(q.w, q.y));
             sz = __fadd_rn(sz, __fmul_rn(q.w, q.z));
             if (kQuad) mom.add(q, box);
-        }
+        });
         reinterpret_cast<float4*>(a.node_sum)[j] = make_float4(sx, sy, sz, m);
         cm = com_from_sums(sx, sy, sz, m);
     } else {
@@ -523,15 +538,14 @@ __device__ __forceinline__ void aggregate_leaf_node_q(const AggArgs& a, uint32_t
         // product of two floats is exact in FP64, so each FMA rounds once,
         // exactly as a multiply-then-add would.
         double m = 0, sx = 0, sy = 0, sz = 0;
-        for (uint32_t i = pb; i < pe; ++i) {
-            const float4 q = a.pos[i];
+        for_particles(a.pos, pb, pe, [&](const float4 q) {
             const double mi = (double)q.w;
             m = __dadd_rn(m, mi);
             sx = __fma_rn(mi, (double)q.x, sx);
             sy = __fma_rn(mi, (double)q.y, sy);
             sz = __fma_rn(mi, (double)q.z, sz);
             if (kQuad) mom.add(q, box);
-        }
+        });
         reinterpret_cast<double4*>(a.node_sum)[j] = make_double4(sx, sy, sz, m);
         if (pe - pb == 1 && m >= 1.17549435e-38) {
             // One particle of normal FP32 mass: the sums are m*x exactly and
