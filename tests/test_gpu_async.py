@@ -78,6 +78,68 @@ def test_pipelined_transfers_match_the_synchronous_calls(native, form, steps):
         assert np.array_equal(gp, wp) and np.array_equal(gv, wv)
 
 
+def test_pipelined_transfers_batched_systems(native):
+    """Systems laid out by astro_upload_systems: the asynchronous uploads keep
+    that layout."""
+    from astro_gb300 import ic
+
+    ag = native
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_PHYSICAL, softening=0.01, far_ratio=0.25)
+    sizes = [3000, 17, 5000, 1, 900]
+    inputs = []
+    for seed in (5, 6):
+        parts = [ic.plummer(s, seed=seed, system=k) for k, s in enumerate(sizes)]
+        inputs.append((np.concatenate([a for a, _ in parts]), np.concatenate([b for _, b in parts])))
+    n = sum(sizes)
+    want = []
+    with ag.Simulation(p, max_n=n, max_systems=len(sizes)) as sim:
+        for pm, vr in inputs:
+            sim.upload_systems(pm.copy(), vr.copy(), sizes)
+            sim.draw(1e-3, 1)
+            want.append(sim.download())
+    outs = [(np.zeros(n, L.POSITION_MASS), np.zeros(n, L.VELOCITY_RADIUS)) for _ in inputs]
+    with ag.Simulation(p, max_n=n, max_systems=len(sizes)) as sim:
+        sim.upload_systems(inputs[0][0].copy(), inputs[0][1].copy(), sizes)
+        for (pm, vr), (opm, ovr) in zip(inputs, outs):
+            sim.upload_async(pm, vr)
+            sim.draw(1e-3, 1)
+            sim.download_async(opm, ovr)
+        sim.synchronize()
+    for (gp, gv), (wp, wv) in zip(outs, want):
+        assert np.array_equal(gp, wp) and np.array_equal(gv, wv)
+
+
+def test_pipelined_transfers_keep_reference_types(native):
+    """REFERENCE preset: the asynchronous uploads keep the particle types and
+    colours of the last synchronous upload (stars, planets, dust)."""
+    from astro_gb300 import ic
+
+    ag = native
+    L = ag.layouts
+    p = ag.default_params(L.PRESET_REFERENCE)
+    pm0, vr0, ct = ic.reference_scene(5, 200, 3000, seed=7)
+    pm1, vr1, _ = ic.reference_scene(5, 200, 3000, seed=8)
+    inputs = [(pm0, vr0), (pm1, vr1)]
+    n = len(pm0)
+    want = []
+    with ag.Simulation(p, max_n=n) as sim:
+        for pm, vr in inputs:
+            sim.upload(pm.copy(), vr.copy(), ct, n_tree=205)
+            sim.draw(1 / 60, 1)
+            want.append(sim.download())
+    outs = [(np.zeros(n, L.POSITION_MASS), np.zeros(n, L.VELOCITY_RADIUS)) for _ in inputs]
+    with ag.Simulation(p, max_n=n) as sim:
+        sim.upload(pm0.copy(), vr0.copy(), ct, n_tree=205)
+        for (pm, vr), (opm, ovr) in zip(inputs, outs):
+            sim.upload_async(pm, vr)
+            sim.draw(1 / 60, 1)
+            sim.download_async(opm, ovr)
+        sim.synchronize()
+    for (gp, gv), (wp, wv) in zip(outs, want):
+        assert np.array_equal(gp, wp) and np.array_equal(gv, wv)
+
+
 def test_overflow_under_pipelined_transfers_is_reported_then_the_batch_runs(native):
     ag = native
     p = _params(ag)

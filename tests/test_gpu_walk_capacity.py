@@ -28,13 +28,13 @@ def _capacity(sim, blocks=0, frontier=0):
     return b.value, f.value, r.value
 
 
-def _case(ag, form, batched, no_graph):
+def _case(ag, form, batched, no_graph, node_list=False):
     from astro_gb300 import ic
 
     L = ag.layouts
     flags = L.FLAG_OPEN_DELTA | L.FLAG_QUADRUPOLE | (L.FLAG_NO_GRAPH if no_graph else 0)
     p = ag.default_params(L.PRESET_PHYSICAL, form=form, softening=0.005, lbits=10, far_ratio=0.2,
-                          flags=flags)
+                          flags=flags, walk_frontier=1 if node_list else 0)
     if batched:
         sizes = [3000, 17, 9000, 1, 5000]
         parts = [ic.plummer(s, seed=11, system=k) for k, s in enumerate(sizes)]
@@ -72,18 +72,19 @@ def test_readbacks_wait_for_the_rerun(native):
     assert np.array_equal(got["acc"], want["acc"]) and got["capacity"][2] >= 2
 
 
-@pytest.mark.parametrize("form,batched,no_graph,blocks,frontier", [
-    ("plain", False, False, 1, 0),      # the list pool: one block
-    ("plain", False, False, 0, 2),      # the frontier: one run
-    ("precision", False, True, 1, 2),   # both, steps launched one by one
-    ("plain", True, False, 40, 8),      # systems batched into one step
+@pytest.mark.parametrize("form,batched,no_graph,blocks,frontier,node_list", [
+    ("plain", False, False, 1, 0, False),      # the list pool: one block
+    ("plain", False, False, 0, 2, False),      # the frontier: one run
+    ("plain", False, False, 0, 2, True),       # the node-list frontier: two nodes
+    ("precision", False, True, 1, 2, False),   # both, steps launched one by one
+    ("plain", True, False, 40, 8, False),      # systems batched into one step
 ])
 def test_steps_rerun_after_the_walk_ran_out_of_room(native, form, batched, no_graph, blocks,
-                                                    frontier):
+                                                    frontier, node_list):
     ag = native
     L = ag.layouts
     p, pm, vr, sizes = _case(ag, L.FORM_PRECISION if form == "precision" else L.FORM_PLAIN,
-                             batched, no_graph)
+                             batched, no_graph, node_list)
     want = _run(ag, p, pm.copy(), vr.copy(), sizes, 3)
     got = _run(ag, p, pm.copy(), vr.copy(), sizes, 3, blocks, frontier)
     for a, b in zip(got["state"], want["state"]):
