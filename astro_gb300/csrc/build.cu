@@ -572,7 +572,7 @@ __device__ __forceinline__ void aggregate_leaf_node_q(const AggArgs& a, uint32_t
         const uint32_t c = pe - pb > gs ? (pe - pb + gs - 1u) / gs : 0u;
         const uint32_t slot = reserve_groups(a.group_count, c);
         for (uint32_t i = 0; i < c; ++i)
-            a.groups[slot + i] = make_uint2(pb + i * gs, min(pb + (i + 1u) * gs, pe));
+            a.groups[slot + i] = make_uint4(pb + i * gs, min(pb + (i + 1u) * gs, pe), pe, i);
     }
 }
 
@@ -781,7 +781,7 @@ __device__ __forceinline__ void aggregate_internal_node(const AggArgs& a, uint32
         uint32_t c = 0;
         pack([&](uint32_t, uint32_t) { ++c; });
         uint32_t slot = reserve_groups(a.group_count, c);
-        pack([&](uint32_t b, uint32_t e) { a.groups[slot++] = make_uint2(b, e); });
+        pack([&](uint32_t b, uint32_t e) { a.groups[slot++] = make_uint4(b, e, e, 0u); });
     }
 }
 

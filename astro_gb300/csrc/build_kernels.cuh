@@ -43,7 +43,13 @@ struct AggArgs {
     float* node_crit2;
     float4* node_q;        // Qxx, Qyy, Qxy, Qxz
     float* node_qyz;       // Qyz
-    uint2* groups;         // particle ranges of the group walk
+    // Groups of the group walk, one record each: (first particle, end
+    // particle, walk end, chunk index). A leaf holding more particles than
+    // a group is cut into consecutive chunks that share one walk against the
+    // whole leaf's box: chunk k's walk starts at its first chunk (record
+    // index - k), whose walk range is [first, walk end) = the leaf. Every
+    // other group walks its own range (walk end = end, chunk index 0).
+    uint4* groups;
     uint32_t* group_count;
     // REFERENCE: star colours (ColorType colour of type-0 particles) summed
     // into each node's emittedColor and averaged into emittedColorCenter
@@ -133,7 +139,7 @@ struct TraverseArgs {
     const float* node_crit2;
     const float4* node_q;
     const float* node_qyz;
-    const uint2* groups;
+    const uint4* groups;      // group walk: (first, end, walk end, chunk index), see AggArgs
     const uint32_t* group_count;
     uint32_t* frontier;       // group walk: per-warp frontier ping-pong buffers,
                               // 2 * frontier_cap words each

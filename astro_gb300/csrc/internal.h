@@ -152,7 +152,7 @@ struct astro_ctx {
     float4* node_ecen = nullptr;      // REFERENCE: emittedColorCenter per node
     float4* node_q = nullptr;         // quadrupole Qxx, Qyy, Qxy, Qxz
     float* node_qyz = nullptr;        // quadrupole Qyz
-    uint2* groups = nullptr;          // group-walk particle ranges (<= n)
+    uint4* groups = nullptr;          // group-walk records (<= n)
     uint32_t* frontier = nullptr;     // group-walk per-warp frontier buffers
     size_t frontier_words = 0;
     uint32_t frontier_cap = 16384;   // words per frontier buffer (set by astro_create)

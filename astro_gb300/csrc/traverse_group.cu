@@ -3,9 +3,12 @@
 // Morton-sorted particles, in two kernels.
 //
 // group_walk_kernel — one warp per group of at most 64 particles (a tree
-//   cell or a pack of sibling cells, emitted with the tree). The warp walks
+//   cell or a pack of sibling cells, emitted with the tree); the chunks a
+//   leaf larger than a group is cut into share one walk against the whole
+//   leaf's box (its particles are in no spatial order inside the leaf, so
+//   each chunk's box is nearly the leaf's anyway). The warp walks
 //   the tree breadth first from the system's root, testing 32 frontier nodes
-//   at a time against the group's bounding box: an accepted node goes to the
+//   at a time against the walk's bounding box: an accepted node goes to the
 //   cell list, or to the far list when its centre of mass lies further than
 //   r_g / far_ratio from the box centre (r_g the box's half diagonal); an
 //   opened leaf or bucket goes to the leaf list; any other opened node puts
@@ -180,15 +183,27 @@ __global__ __launch_bounds__(kWalkWarps * 32, kWalkWarpsPerSm / kWalkWarps) void
         gi = __shfl_sync(kFullMask, gi, 0);
         if (gi >= ngroups) break;
         gi = group_of_ticket(gi, ngroups, a.group_chunk);
-        const uint2 gr = a.groups[gi];
-        const uint32_t gcount = gr.y - gr.x;
-        // Group bounding box over up to 64 particles (two per lane).
-        const bool v0 = lane < gcount, v1 = lane + 32u < gcount;
-        const float4 p0 = v0 ? a.pos[gr.x + lane] : make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-        const float4 p1 = v1 ? a.pos[gr.x + 32u + lane] : p0;
-        float lo_x = fminf(p0.x, p1.x), lo_y = fminf(p0.y, p1.y), lo_z = fminf(p0.z, p1.z);
-        float hi_x = v0 ? fmaxf(p0.x, p1.x) : -INFINITY, hi_y = v0 ? fmaxf(p0.y, p1.y) : -INFINITY,
-              hi_z = v0 ? fmaxf(p0.z, p1.z) : -INFINITY;
+        const uint4 gr = a.groups[gi];
+        // Later chunks of a leaf use the walk of its first chunk.
+        if (gr.w != 0u) continue;
+        // The walk's box: the group, or the whole leaf a first chunk stands
+        // for (any number of particles, 64 at a time).
+        const uint32_t wcount = gr.z - gr.x;
+        float lo_x = INFINITY, lo_y = INFINITY, lo_z = INFINITY;
+        float hi_x = -INFINITY, hi_y = -INFINITY, hi_z = -INFINITY;
+        for (uint32_t b = 0; b < wcount; b += 64u) {
+            const bool v0 = b + lane < wcount, v1 = b + 32u + lane < wcount;
+            if (v0) {
+                const float4 p0 = a.pos[gr.x + b + lane];
+                lo_x = fminf(lo_x, p0.x), lo_y = fminf(lo_y, p0.y), lo_z = fminf(lo_z, p0.z);
+                hi_x = fmaxf(hi_x, p0.x), hi_y = fmaxf(hi_y, p0.y), hi_z = fmaxf(hi_z, p0.z);
+            }
+            if (v1) {
+                const float4 p1 = a.pos[gr.x + b + 32u + lane];
+                lo_x = fminf(lo_x, p1.x), lo_y = fminf(lo_y, p1.y), lo_z = fminf(lo_z, p1.z);
+                hi_x = fmaxf(hi_x, p1.x), hi_y = fmaxf(hi_y, p1.y), hi_z = fmaxf(hi_z, p1.z);
+            }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             lo_x = fminf(lo_x, __shfl_xor_sync(kFullMask, lo_x, o));
@@ -361,8 +376,11 @@ __global__ __launch_bounds__(kWalkWarps * 32, kWalkWarpsPerSm / kWalkWarps) void
                 if (lane == (uint32_t)k) v = w[k];
             reinterpret_cast<uint32_t*>(a.desc + gi)[lane] = v;
         }
-        visits += (unsigned long long)gcount * tested;
-        far_nodes += fars.count;
+        // Per particle of the walk, and one expansion per group and far
+        // node (the chunks sharing this walk: all but the last hold
+        // gr.y - gr.x particles).
+        visits += (unsigned long long)wcount * tested;
+        far_nodes += (unsigned long long)fars.count * ((wcount + (gr.y - gr.x) - 1u) / (gr.y - gr.x));
     }
     if (lane == 0) {
         atomicAdd(&a.stats[1], visits);
@@ -928,8 +946,9 @@ __global__ ASTRO_EVAL_BOUNDS(kWarps) void group_eval_kernel(TraverseArgs a) {
         gi = __shfl_sync(kFullMask, gi, 0);
         if (gi >= ngroups) break;
         gi = group_of_ticket(gi, ngroups, a.group_chunk);
-        const uint2 gr = a.groups[gi];
-        const GroupDesc d = a.desc[gi];
+        const uint4 rec = a.groups[gi];
+        const uint2 gr = make_uint2(rec.x, rec.y);
+        const GroupDesc d = a.desc[gi - rec.w];  // the walk of the leaf's first chunk
         if (gr.y - gr.x > 32u)
             eval_group<kExact, kPrec, kQuad, kCellCap, 2, kPipe>(a, gr, d, s_cell[warp], s_tile[warp],
                                                                  s_jdx[warp], lane, inter,

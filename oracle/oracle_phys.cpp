@@ -561,20 +561,26 @@ struct PhysState {
     //  - a node with more than kGroup particles packs its consecutive small
     //    children (at most kGroup particles each) greedily, in child order;
     //  - a top-layer node with at most kGroup particles is a group;
-    //  - a leaf with more than kGroup particles is cut into kGroup chunks.
-    std::vector<std::pair<uint32_t, uint32_t>> make_groups() const {
+    //  - a leaf with more than kGroup particles is cut into kGroup chunks,
+    //    which are walked against the box of the whole leaf.
+    // Each group: its particles [first, second) and the particles [wb, we)
+    // whose bounding box its walk tests.
+    struct Group {
+        uint32_t first, second, wb, we;
+    };
+    std::vector<Group> make_groups() const {
         const uint32_t kGroup = p.group_size ? p.group_size : kDefaultGroup;
-        std::vector<std::pair<uint32_t, uint32_t>> groups;
+        std::vector<Group> groups;
         for (uint32_t l = 0; l < layers; ++l)
             for (uint32_t k = 0; k < counts[l]; ++k) {
                 uint32_t node = offsets[l] + k, pc = pend[node] - pbeg[node];
                 if (pc <= kGroup) {
-                    if (l == lbits) groups.push_back({pbeg[node], pend[node]});
+                    if (l == lbits) groups.push_back({pbeg[node], pend[node], pbeg[node], pend[node]});
                     continue;
                 }
                 if (l == 0) {
                     for (uint32_t b = pbeg[node]; b < pend[node]; b += kGroup)
-                        groups.push_back({b, std::min(b + kGroup, pend[node])});
+                        groups.push_back({b, std::min(b + kGroup, pend[node]), pbeg[node], pend[node]});
                     continue;
                 }
                 uint32_t gb = 0, ge = 0;
@@ -587,16 +593,16 @@ struct PhysState {
                         } else if ((ge - gb) + cc <= kGroup) {
                             ge = pend[ch];
                         } else {
-                            groups.push_back({gb, ge});
+                            groups.push_back({gb, ge, gb, ge});
                             gb = pbeg[ch];
                             ge = pend[ch];
                         }
                     } else if (ge != gb) {
-                        groups.push_back({gb, ge});
+                        groups.push_back({gb, ge, gb, ge});
                         gb = ge = 0;
                     }
                 }
-                if (ge != gb) groups.push_back({gb, ge});
+                if (ge != gb) groups.push_back({gb, ge, gb, ge});
             }
         return groups;
     }
@@ -626,7 +632,7 @@ struct PhysState {
             const uint32_t gb = groups[gi].first, ge = groups[gi].second;
             const uint32_t s = sys_of[gb];
             float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (uint32_t i = gb; i < ge; ++i)
+            for (uint32_t i = groups[gi].wb; i < groups[gi].we; ++i)
                 for (int a = 0; a < 3; ++a) {
                     lo[a] = std::min(lo[a], rel[4ull * i + a]);
                     hi[a] = std::max(hi[a], rel[4ull * i + a]);

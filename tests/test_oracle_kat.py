@@ -447,16 +447,18 @@ def test_far_nodes_keep_the_walk_and_the_accuracy(oracle, native):
 
 
 def test_far_ratio_one_particle_groups_and_systems(oracle, native):
-    # Groups of one particle (box of zero size): every accepted node is far,
-    # in every system of a batch.
+    # Groups of one particle walked alone (box of zero size: leaves of one
+    # particle at 20 bits per axis, so no leaf is cut into chunks that share
+    # a walk): every accepted node is far, in every system of a batch.
     from astro_gb300 import ic
 
     sizes = [1, 2, 300, 1000]
     parts = [ic.plummer(s, seed=1004, system=k) for k, s in enumerate(sizes)]
     pm = np.concatenate([a for a, _ in parts])
     vr = np.concatenate([b for _, b in parts])
-    near = oracle.phys_run(phys_params(group_size=1), pm.copy(), vr.copy(), sizes=sizes, dt=0.0)
-    far = oracle.phys_run(phys_params(group_size=1, far_ratio=0.5), pm.copy(), vr.copy(),
+    near = oracle.phys_run(phys_params(group_size=1, lbits=20), pm.copy(), vr.copy(), sizes=sizes,
+                           dt=0.0)
+    far = oracle.phys_run(phys_params(group_size=1, lbits=20, far_ratio=0.5), pm.copy(), vr.copy(),
                           sizes=sizes, dt=0.0)
     assert far["interactions"] == near["interactions"]
     assert far["far_nodes"] == far["far_interactions"] > 0
