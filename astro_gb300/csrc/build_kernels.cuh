@@ -98,6 +98,7 @@ struct GroupDesc {
     uint32_t far_first, n_far;
     float gcx, gcy, gcz;
     uint32_t pad[3];
+    float far_co[20];  // the far nodes' summed expansion coefficients (19 used)
 };
 
 struct TraverseArgs {
@@ -252,6 +253,8 @@ struct TraverseConfig {
     bool persistent;  // persistent blocks with a work-stealing chunk queue
     int warps;        // warps per block (2, 4 or 8)
     bool quad;        // quadrupole terms (group walk template switch)
+    bool far_pre;     // group walk: far-node sums once per walk in group_far_kernel
+                      // (groups of more than 32), else in each group's evaluation
 };
 cudaError_t launch_traverse_ref(const TraverseArgs& a, cudaStream_t st);
 cudaError_t launch_traverse_phys(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st);

@@ -270,6 +270,11 @@ astro::TraverseConfig traverse_config(const astro_ctx* ctx) {
     c.persistent = (ctx->p.flags & ASTRO_FLAG_PERSISTENT) != 0;
     c.warps = ctx->p.block_warps ? (int)ctx->p.block_warps : 4;
     c.quad = (ctx->p.flags & ASTRO_FLAG_QUADRUPOLE) != 0;
+    // Far-node sums once per walk for groups of more than 32 (measured
+    // faster there: the evaluation of two particles per lane holds fewer
+    // values, and the chunks of a leaf share the sums); in each group's
+    // evaluation otherwise.
+    c.far_pre = ctx->p.far_ratio > 0.f && ctx->p.group_size > 32;
     return c;
 }
 

@@ -376,15 +376,68 @@ __global__ __launch_bounds__(kWalkWarps * 32, kWalkWarpsPerSm / kWalkWarps) void
                 if (lane == (uint32_t)k) v = w[k];
             reinterpret_cast<uint32_t*>(a.desc + gi)[lane] = v;
         }
-        // Per particle of the walk, and one expansion per group and far
-        // node (the chunks sharing this walk: all but the last hold
-        // gr.y - gr.x particles).
+        // Per particle of the walk; one expansion per walk and far node.
         visits += (unsigned long long)wcount * tested;
-        far_nodes += (unsigned long long)fars.count * ((wcount + (gr.y - gr.x) - 1u) / (gr.y - gr.x));
+        far_nodes += fars.count;
     }
     if (lane == 0) {
         atomicAdd(&a.stats[1], visits);
         if (far_nodes) atomicAdd(&a.stats[3], far_nodes);
+    }
+}
+
+// ------------------------------------------------------------ far nodes --
+
+// The far-node expansion of every walk, once: lane l sums the coefficients
+// of far nodes l, l + 32, ... in walk order; the partials are combined
+// pairwise (lane l + lane l^o, o = 16 .. 1), leaving the sum in every lane;
+// the 19 sums go into the walk's record, where the evaluation of each group
+// sharing the walk reads them. One warp per record, records in order.
+template <bool kExact, bool kQuad>
+__global__ __launch_bounds__(128) void group_far_kernel(TraverseArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    // A walk that ran out of room left incomplete lists: nothing to expand.
+    if (*reinterpret_cast<volatile const uint32_t*>(a.err) & kErrFrontier) return;
+    const uint32_t ngroups = *a.group_count;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32u);
+    const float eps2 = a.eps2;
+    for (uint32_t gi = blockIdx.x * (blockDim.x / 32u) + (threadIdx.x >> 5); gi < ngroups;
+         gi += nwarps) {
+        if (a.groups[gi].w != 0u) continue;  // a later chunk: no walk of its own
+        GroupDesc* const dp = a.desc + gi;
+        const uint32_t n_far = dp->n_far;
+        if (n_far == 0u) continue;
+        const float gcx = dp->gcx, gcy = dp->gcy, gcz = dp->gcz;
+        float fc[kFarCoefs];
+#pragma unroll
+        for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
+        // Far node f sits at position f mod 64 of block f / 64 of the chain.
+        ChainCursor cur{dp->far_first};
+        for (uint32_t f = lane; f < n_far; f += 32u) {
+            if (f >= kListBlockWords && (f % kListBlockWords) < 32u) cur.advance(a);
+            const uint32_t nd = cur.words(a)[f % kListBlockWords];
+            const float4 c = __ldg(&a.node_cm[nd]);
+            if constexpr (kQuad) {
+                const float4 q = __ldg(&a.node_q[nd]);
+                far_coefs<kExact, true>(c, q, __ldg(&a.node_qyz[nd]), -(q.x + q.y), gcx, gcy, gcz, eps2,
+                                        fc);
+            } else {
+                far_coefs<kExact, false>(c, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, gcx, gcy, gcz,
+                                         eps2, fc);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kFarCoefs; ++k) {
+            float v = fc[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v = xadd<kExact>(v, __shfl_xor_sync(kFullMask, v, o));
+            fc[k] = v;
+        }
+        float v = fc[0];
+#pragma unroll
+        for (int k = 1; k < kFarCoefs; ++k)
+            if (lane == (uint32_t)k) v = fc[k];
+        if (lane < (uint32_t)kFarCoefs) dp->far_co[lane] = v;
     }
 }
 
@@ -394,8 +447,9 @@ namespace {
 
 // Evaluation of one group whose particles sit kPer per lane (kPer = 2:
 // particles lane and lane + 32). Adds this lane's interaction counts.
-template <bool kExact, bool kPrec, bool kQuad, int kCellCap, int kPer, bool kPipe>
+template <bool kExact, bool kPrec, bool kQuad, int kCellCap, int kPer, bool kPipe, bool kFarPre>
 __device__ __forceinline__ void eval_group(const TraverseArgs& a, const uint2 gr, const GroupDesc& d,
+                                           const float* __restrict__ far_co,
                                            CellSlot<kQuad>* s_cell, float4* s_tile, uint32_t* s_jdx,
                                            uint32_t lane, uint32_t& inter, uint32_t& cell_inter,
                                            uint32_t& far_inter) {
@@ -444,29 +498,42 @@ __device__ __forceinline__ void eval_group(const TraverseArgs& a, const uint2 gr
     for (int k = 0; k < kPer; ++k) fx[k] = fy[k] = fz[k] = 0.f;
     if (d.n_far > 0) {
         float fc[kFarCoefs];
+        if constexpr (kFarPre) {
+            // The walk's summed coefficients (group_far_kernel), the same for
+            // every chunk that shares the walk.
+            float buf[kFarCoefs + 1];
 #pragma unroll
-        for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
-        // Far node f sits at position f mod 64 of block f / 64 of the chain.
-        ChainCursor cur{d.far_first};
-        for (uint32_t f = lane; f < d.n_far; f += 32u) {
-            if (f >= kListBlockWords && (f % kListBlockWords) < 32u) cur.advance(a);
-            const uint32_t nd = cur.words(a)[f % kListBlockWords];
-            const float4 c = __ldg(&a.node_cm[nd]);
-            if constexpr (kQuad) {
-                const float4 q = __ldg(&a.node_q[nd]);
-                far_coefs<kExact, true>(c, q, __ldg(&a.node_qyz[nd]), -(q.x + q.y), gcx, gcy, gcz, eps2,
-                                        fc);
-            } else {
-                far_coefs<kExact, false>(c, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, gcx, gcy, gcz,
-                                         eps2, fc);
+            for (int k = 0; k < (kFarCoefs + 1) / 4; ++k) {
+                const float4 v = __ldg(reinterpret_cast<const float4*>(far_co) + k);
+                buf[4 * k] = v.x, buf[4 * k + 1] = v.y, buf[4 * k + 2] = v.z, buf[4 * k + 3] = v.w;
             }
-        }
 #pragma unroll
-        for (int k = 0; k < kFarCoefs; ++k) {
-            float v = fc[k];
+            for (int k = 0; k < kFarCoefs; ++k) fc[k] = buf[k];
+        } else {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v = xadd<kExact>(v, __shfl_xor_sync(kFullMask, v, o));
-            fc[k] = v;
+            for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
+            // Far node f sits at position f mod 64 of block f / 64 of the chain.
+            ChainCursor cur{d.far_first};
+            for (uint32_t f = lane; f < d.n_far; f += 32u) {
+                if (f >= kListBlockWords && (f % kListBlockWords) < 32u) cur.advance(a);
+                const uint32_t nd = cur.words(a)[f % kListBlockWords];
+                const float4 c = __ldg(&a.node_cm[nd]);
+                if constexpr (kQuad) {
+                    const float4 q = __ldg(&a.node_q[nd]);
+                    far_coefs<kExact, true>(c, q, __ldg(&a.node_qyz[nd]), -(q.x + q.y), gcx, gcy, gcz, eps2,
+                                            fc);
+                } else {
+                    far_coefs<kExact, false>(c, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, gcx, gcy, gcz,
+                                             eps2, fc);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kFarCoefs; ++k) {
+                float v = fc[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v = xadd<kExact>(v, __shfl_xor_sync(kFullMask, v, o));
+                fc[k] = v;
+            }
         }
 #pragma unroll
         for (int k = 0; k < kPer; ++k)
@@ -920,7 +987,7 @@ __device__ __forceinline__ void eval_group(const TraverseArgs& a, const uint2 gr
 #define ASTRO_EVAL_BOUNDS(w) __launch_bounds__((w) * 32)
 #endif
 
-template <bool kExact, bool kPrec, bool kQuad, int kWarps>
+template <bool kExact, bool kPrec, bool kQuad, int kWarps, bool kFarPre>
 __global__ ASTRO_EVAL_BOUNDS(kWarps) void group_eval_kernel(TraverseArgs a) {
     constexpr int kCellCap = cell_cap(kWarps);
     // Leaf tiles loaded one tile ahead with 4-warp blocks; the 8-warp blocks
@@ -948,13 +1015,23 @@ __global__ ASTRO_EVAL_BOUNDS(kWarps) void group_eval_kernel(TraverseArgs a) {
         gi = group_of_ticket(gi, ngroups, a.group_chunk);
         const uint4 rec = a.groups[gi];
         const uint2 gr = make_uint2(rec.x, rec.y);
-        const GroupDesc d = a.desc[gi - rec.w];  // the walk of the leaf's first chunk
+        // The walk of the leaf's first chunk: its lists and centre (the first
+        // 48 bytes of the record) and its far-node coefficients.
+        const GroupDesc* dp = a.desc + (gi - rec.w);
+        GroupDesc d;
+        {
+            const uint4* w = reinterpret_cast<const uint4*>(dp);
+            const uint4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
+            d.leaf_first = w0.x, d.n_leaf = w0.y, d.cell_first = w0.z, d.n_cell = w0.w;
+            d.far_first = w1.x, d.n_far = w1.y, d.gcx = __uint_as_float(w1.z);
+            d.gcy = __uint_as_float(w1.w), d.gcz = __uint_as_float(w2.x);
+        }
         if (gr.y - gr.x > 32u)
-            eval_group<kExact, kPrec, kQuad, kCellCap, 2, kPipe>(a, gr, d, s_cell[warp], s_tile[warp],
+            eval_group<kExact, kPrec, kQuad, kCellCap, 2, kPipe, kFarPre>(a, gr, d, dp->far_co, s_cell[warp], s_tile[warp],
                                                                  s_jdx[warp], lane, inter,
                                                                  cell_inter, far_inter);
         else
-            eval_group<kExact, kPrec, kQuad, kCellCap, 1, kPipe>(a, gr, d, s_cell[warp], s_tile[warp],
+            eval_group<kExact, kPrec, kQuad, kCellCap, 1, kPipe, kFarPre>(a, gr, d, dp->far_co, s_cell[warp], s_tile[warp],
                                                                  s_jdx[warp], lane, inter,
                                                                  cell_inter, far_inter);
     }
@@ -1014,9 +1091,9 @@ uint32_t walk_blocks() {
     return (uint32_t)per_sm * (uint32_t)sm_count();
 }
 
-template <bool kExact, bool kPrec, bool kQuad, int kWarps>
+template <bool kExact, bool kPrec, bool kQuad, int kWarps, bool kFarPre>
 cudaError_t launch_eval_t(const TraverseArgs& a, cudaStream_t st) {
-    auto kernel = group_eval_kernel<kExact, kPrec, kQuad, kWarps>;
+    auto kernel = group_eval_kernel<kExact, kPrec, kQuad, kWarps, kFarPre>;
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, 0);
     if (e != cudaSuccess) return e;
@@ -1025,16 +1102,19 @@ cudaError_t launch_eval_t(const TraverseArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-template <bool kExact, bool kPrec, bool kQuad>
+template <bool kExact, bool kPrec, bool kQuad, bool kFarPre>
 cudaError_t launch_eval_w(const TraverseArgs& a, int warps, cudaStream_t st) {
-    return warps == 8 ? launch_eval_t<kExact, kPrec, kQuad, 8>(a, st)
-                      : launch_eval_t<kExact, kPrec, kQuad, 4>(a, st);
+    return warps == 8 ? launch_eval_t<kExact, kPrec, kQuad, 8, kFarPre>(a, st)
+                      : launch_eval_t<kExact, kPrec, kQuad, 4, kFarPre>(a, st);
 }
 
 template <bool kExact, bool kPrec>
 cudaError_t launch_eval_q(const TraverseArgs& a, const TraverseConfig& c, cudaStream_t st) {
-    return c.quad ? launch_eval_w<kExact, kPrec, true>(a, c.warps, st)
-                  : launch_eval_w<kExact, kPrec, false>(a, c.warps, st);
+    if (c.far_pre)
+        return c.quad ? launch_eval_w<kExact, kPrec, true, true>(a, c.warps, st)
+                      : launch_eval_w<kExact, kPrec, false, true>(a, c.warps, st);
+    return c.quad ? launch_eval_w<kExact, kPrec, true, false>(a, c.warps, st)
+                  : launch_eval_w<kExact, kPrec, false, false>(a, c.warps, st);
 }
 
 }  // namespace
@@ -1066,6 +1146,16 @@ cudaError_t launch_traverse_groups(const TraverseArgs& a, const TraverseConfig& 
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (ev && (e = cudaEventRecord(ev[1], st)) != cudaSuccess) return e;
+    if (c.far_pre && a.far2 > 0.f) {
+        const uint32_t blocks = walk_blocks();
+        if (c.exact)
+            c.quad ? group_far_kernel<true, true><<<blocks, 128, 0, st>>>(a)
+                   : group_far_kernel<true, false><<<blocks, 128, 0, st>>>(a);
+        else
+            c.quad ? group_far_kernel<false, true><<<blocks, 128, 0, st>>>(a)
+                   : group_far_kernel<false, false><<<blocks, 128, 0, st>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if (c.exact)
         e = c.precision ? launch_eval_q<true, true>(a, c, st) : launch_eval_q<true, false>(a, c, st);
     else

@@ -55,10 +55,11 @@ UNIT = "particle-updates/s"
 # two vector updates (6), counting an FMA as 2).
 FLOPS_PER_INTERACTION = 20
 FLOPS_PER_QUAD_CELL = 50
-# A far node's expansion about its group's centre: 350 flops once per group
+# A far node's expansion about its walk's centre: 350 flops once per walk
 # (the field, its 6 first and 10 second derivatives from the monopole and
-# quadrupole, and their 19 sums), and 70 per particle of a group with far
-# nodes to evaluate the expansion (3 x (J rho, H rho rho, sums)).
+# quadrupole, and their 19 sums; group_far_kernel, timed with the
+# evaluation), and 70 per particle of a group with far nodes to evaluate
+# the expansion (3 x (J rho, H rho rho, sums)).
 FLOPS_PER_FAR_NODE = 350
 FLOPS_PER_FAR_EVAL = 70
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
@@ -852,7 +853,9 @@ def main(argv=None):
             "e2e": r["e2e"], "gpu_launches": r["launches"],
             "roofline": {"kernel": ("traverse_ref_kernel"
                                     if WORKLOADS[args.workload].preset == "reference"
-                                    else "group_eval_kernel" if group
+                                    else ("group_far_kernel + group_eval_kernel"
+                                          if r["far_nodes"] and r["p"].group_size > 32
+                                          else "group_eval_kernel") if group
                                     else "traverse_phys_kernel"),
                          "bound": "fp32",
                          "achieved": r["achieved"], "peak": r["fp32_peak"], "unit": "TFLOP/s",

@@ -302,7 +302,8 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
                      uint64_t* cell_interactions);
 
 /* Far-node statistics of the last group walk (params.far_ratio > 0): the
- * expansions formed (one per group and far node) and, summed over
+ * expansions formed (one per walk and far node; the chunks of a leaf larger
+ * than a group share one walk) and, summed over
  * particles, the accepted nodes evaluated through them (a part of
  * cell_interactions above). */
 int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions);

@@ -684,7 +684,8 @@ struct PhysState {
                     std::memcpy(part, nxt, sizeof(part));
                 }
                 std::memcpy(fsum, part[0], sizeof(fsum));
-                tot_far_nodes += far.size();
+                // One expansion per walk: the chunks of a leaf share one.
+                if (groups[gi].first == groups[gi].wb) tot_far_nodes += far.size();
             }
             for (uint32_t ip = gb; ip < ge; ++ip) {
                 const float px = rel[4ull * ip], py = rel[4ull * ip + 1], pz = rel[4ull * ip + 2];
