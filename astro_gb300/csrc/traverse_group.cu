@@ -14,13 +14,17 @@
 //   opened leaf or bucket goes to the leaf list; any other opened node puts
 //   its children in the next frontier. Each list is a chain of 64-word
 //   blocks of a shared pool (the warp takes blocks from the pool in batches);
-//   a per-group descriptor records the chains.
+//   a per-walk record holds the chains and the box centre.
+// group_far_kernel — the far nodes' second-order field expansion about the
+//   walk's box centre, once per walk (groups of more than 32): lane l
+//   expands far nodes l, l + 32, ... into its partial of the 19
+//   coefficients, the partials are combined by an xor butterfly (16 .. 1)
+//   and the sums go into the walk's record. Groups of up to 32 form the
+//   same sums in their own evaluation.
 // group_eval_kernel — one warp per group: each lane holds one particle (two
 //   for groups of 33..64; copies of each particle for groups of at most 16
-//   in the fast form). Lane l expands far nodes l, l + 32, ... into its
-//   partial of the 19 coefficients of a second-order field expansion about
-//   the box centre; the partials are combined by an xor butterfly (16 .. 1)
-//   and each particle evaluates the expansion at its offset. Cells are
+//   in the fast form). Each particle evaluates the far-node expansion at
+//   its offset from the box centre. Cells are
 //   gathered into shared memory and summed; the listed leaves' particles are
 //   staged 32 at a time and summed. The epilogue clamps, stores the
 //   acceleration and performs the kick-drift (v += a dt, x += v dt).
