@@ -502,7 +502,8 @@ int stage_traverse(astro_ctx* ctx, float dt, bool integrate) {
     if (group_walk(ctx)) {
         int r = ensure_frontier(ctx);
         if (r != ASTRO_OK) return r;
-        // Stage calls (outside stream capture) time the two kernels.
+        // Stage calls (outside stream capture) time the walk and the
+        // evaluation (with the far-node sums when they run apart).
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         CK(cudaStreamIsCapturing(st, &cap));
         const bool timed = cap == cudaStreamCaptureStatusNone;

@@ -1,6 +1,7 @@
 // Group walk of the PHYSICAL preset: barnesHut (Astro/BarnesHut.metal:22-101)
 // with the opening decisions made once per group of consecutive
-// Morton-sorted particles, in two kernels.
+// Morton-sorted particles, in two kernels (three for groups of more than
+// 32 with far nodes).
 //
 // group_walk_kernel — one warp per group of at most 64 particles (a tree
 //   cell or a pack of sibling cells, emitted with the tree); the chunks a

@@ -524,8 +524,9 @@ def run_ours(args, world, rank, local):
         (FLOPS_PER_FAR_EVAL * n if far_nodes else 0)
 
     # Traversal alone, several launches after a flush each, for the roofline:
-    # the group walk's two kernels timed apart (events recorded by the
-    # library between them), the other walks as one kernel.
+    # the group walk timed apart from its evaluation (the far-node sums
+    # and the evaluation kernel; events recorded by the library between
+    # them), the other walks as one kernel.
     trav_ms, walk_ms, eval_ms = [], [], []
     for _ in range(3):
         with torch.cuda.stream(stream):

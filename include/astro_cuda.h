@@ -308,9 +308,10 @@ int astro_read_stats(astro_ctx* ctx, uint64_t* interactions, uint64_t* node_visi
  * cell_interactions above). */
 int astro_read_far_stats(astro_ctx* ctx, uint64_t* far_nodes, uint64_t* far_interactions);
 
-/* Device times of the two kernels of the last group-walk traversal made by
- * a stage call (astro_traverse; graph-replayed steps are not timed): the
- * walk that builds the interaction lists and the evaluation that sums them
+/* Device times of the last group-walk traversal made by a stage call
+ * (astro_traverse; graph-replayed steps are not timed): the walk that
+ * builds the interaction lists, and the evaluation that sums them
+ * (including the per-walk far-node sums for groups of more than 32)
  * (CUDA events on the context's stream; waits for them). */
 int astro_read_traverse_times(astro_ctx* ctx, float* walk_ms, float* eval_ms);
 

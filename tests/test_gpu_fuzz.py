@@ -54,13 +54,23 @@ def _particles(L, ic, cfg):
     return pm, vr, sizes
 
 
-@pytest.mark.parametrize("k", range(CASES))
+def _large_groups(cfg, k):
+    """Groups of 33 to 64 particles (two per lane; the chunks of a leaf
+    that holds more share one walk, and with far nodes their sums are
+    formed once per walk by their own kernel)."""
+    rng = np.random.default_rng(9700 + k)
+    cfg.update(group_size=int(rng.integers(33, 65)), far_ratio=float(rng.choice([0.0, 0.25, 0.5])),
+               n=int(rng.choice([7, 500, 4097, 12000, 30000])), lbits=int(rng.integers(1, 6)))
+    return cfg
+
+
+@pytest.mark.parametrize("k", range(CASES + 12))
 def test_random_configuration_bit_exact(ag, oracle, k):
     from astro_gb300 import ic
     from test_gpu_parity import assert_tree_equal, run_gpu
 
     L = ag.layouts
-    cfg = _config(k)
+    cfg = _config(k) if k < CASES else _large_groups(_config(k), k)
     flags = L.FLAG_IEEE_EXACT | (L.FLAG_QUADRUPOLE if cfg["quad"] else 0) | (
         L.FLAG_OPEN_DELTA if cfg["delta"] else 0)
     pm, vr, sizes = _particles(L, ic, cfg)
@@ -113,16 +123,17 @@ def test_random_reference_scene_bit_exact(ag, oracle, k):
     assert np.array_equal(out["pm"], pm_o) and np.array_equal(out["vr"], vr_o), cfg
 
 
-@pytest.mark.parametrize("k", range(16))
+@pytest.mark.parametrize("k", range(16 + 8))
 def test_random_configuration_fast_within_tolerance(ag, oracle, k):
     """The fast form (rsqrt, FMAs, replicated small groups, factored far-node
-    coefficients) over random configurations: the same walk (identical
-    counts) and accelerations within the fast path's tolerance."""
+    coefficients, groups of up to 64 in packed pairs) over random
+    configurations: the same walk (identical counts) and accelerations
+    within the fast path's tolerance."""
     from astro_gb300 import ic
     from test_gpu_parity import acc_close, assert_tree_equal, run_gpu
 
     L = ag.layouts
-    cfg = _config(100 + k)
+    cfg = _config(100 + k) if k < 16 else _large_groups(_config(100 + k), 100 + k)
     cfg["n"] = max(cfg["n"], 500)
     flags = (L.FLAG_QUADRUPOLE if cfg["quad"] else 0) | (L.FLAG_OPEN_DELTA if cfg["delta"] else 0)
     pm, vr, sizes = _particles(L, ic, cfg)
