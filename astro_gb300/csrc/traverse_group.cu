@@ -526,20 +526,27 @@ __device__ __forceinline__ void eval_group(const TraverseArgs& a, const uint2 gr
         } else {
 #pragma unroll
             for (int k = 0; k < kFarCoefs; ++k) fc[k] = 0.f;
-            // Far node f sits at position f mod 64 of block f / 64 of the chain.
+            // Far node f sits at position f mod 64 of block f / 64 of the
+            // chain; each lane reads its next node id before expanding node f.
             ChainCursor cur{d.far_first};
+            uint32_t nd = lane < d.n_far ? cur.words(a)[lane] : 0u;
             for (uint32_t f = lane; f < d.n_far; f += 32u) {
-                if (f >= kListBlockWords && (f % kListBlockWords) < 32u) cur.advance(a);
-                const uint32_t nd = cur.words(a)[f % kListBlockWords];
                 const float4 c = __ldg(&a.node_cm[nd]);
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                float qyz = 0.f;
                 if constexpr (kQuad) {
-                    const float4 q = __ldg(&a.node_q[nd]);
-                    far_coefs<kExact, true>(c, q, __ldg(&a.node_qyz[nd]), -(q.x + q.y), gcx, gcy, gcz, eps2,
-                                            fc);
-                } else {
-                    far_coefs<kExact, false>(c, make_float4(0.f, 0.f, 0.f, 0.f), 0.f, 0.f, gcx, gcy, gcz,
-                                             eps2, fc);
+                    q = __ldg(&a.node_q[nd]);
+                    qyz = __ldg(&a.node_qyz[nd]);
                 }
+                const uint32_t fn = f + 32u;
+                if (fn < d.n_far) {
+                    if ((fn % kListBlockWords) < 32u) cur.advance(a);
+                    nd = cur.words(a)[fn % kListBlockWords];
+                }
+                if constexpr (kQuad)
+                    far_coefs<kExact, true>(c, q, qyz, -(q.x + q.y), gcx, gcy, gcz, eps2, fc);
+                else
+                    far_coefs<kExact, false>(c, q, 0.f, 0.f, gcx, gcy, gcz, eps2, fc);
             }
 #pragma unroll
             for (int k = 0; k < kFarCoefs; ++k) {
