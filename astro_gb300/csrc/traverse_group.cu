@@ -51,9 +51,18 @@ constexpr int kWalkWarps = 4;
 constexpr int kWalkWarpsPerSm = 32;
 constexpr uint32_t kNoBlock = 0xFFFFFFFFu;
 
-// Resident warps per SM the evaluation's register allocation is sized for.
+// Resident warps per SM the evaluation's register allocation is sized for:
+// 24 (80 registers, a few spilled), except the plain form's 8-warp blocks
+// at 16 (up to 128 registers, none spilled). Measured: the plain C3 and C1
+// lines (8-warp blocks) 4.86 -> 4.79 ms and 0.251 -> 0.241 ms at 16; the
+// precision form's 8-warp blocks lost at 16 (C5 18.9 -> 19.3 ms, C2 1.40
+// -> 1.48 ms); 4-warp blocks at C5 and C4 ran best at 24 (17.32 and 7.33
+// ms, against 17.46 and 7.47 at 20 and 17.38 and 7.54 at 28).
 #ifndef ASTRO_GROUP_WARPS_PER_SM
 #define ASTRO_GROUP_WARPS_PER_SM 24
+#endif
+#ifndef ASTRO_GROUP_WARPS_PER_SM_8
+#define ASTRO_GROUP_WARPS_PER_SM_8 16
 #endif
 
 // Cell records staged per warp (the evaluation's shared memory): two list
@@ -1003,13 +1012,16 @@ __device__ __forceinline__ void eval_group(const TraverseArgs& a, const uint2 gr
 }  // namespace
 
 #if ASTRO_GROUP_WARPS_PER_SM > 0
-#define ASTRO_EVAL_BOUNDS(w) __launch_bounds__((w) * 32, ASTRO_GROUP_WARPS_PER_SM / (w))
+#define ASTRO_EVAL_BOUNDS(w, prec)                                                            \
+    __launch_bounds__((w) * 32,                                                              \
+                      ((w) >= 8 && !(prec) ? ASTRO_GROUP_WARPS_PER_SM_8 : ASTRO_GROUP_WARPS_PER_SM) / \
+                          (w))
 #else
-#define ASTRO_EVAL_BOUNDS(w) __launch_bounds__((w) * 32)
+#define ASTRO_EVAL_BOUNDS(w, prec) __launch_bounds__((w) * 32)
 #endif
 
 template <bool kExact, bool kPrec, bool kQuad, int kWarps, bool kFarPre>
-__global__ ASTRO_EVAL_BOUNDS(kWarps) void group_eval_kernel(TraverseArgs a) {
+__global__ ASTRO_EVAL_BOUNDS(kWarps, kPrec) void group_eval_kernel(TraverseArgs a) {
     constexpr int kCellCap = cell_cap(kWarps);
     // Leaf tiles loaded one tile ahead with 4-warp blocks; the 8-warp blocks
     // (half the cell staging per warp) keep the load in line, which measured
