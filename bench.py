@@ -64,11 +64,12 @@ FLOPS_PER_FAR_NODE = 350
 FLOPS_PER_FAR_EVAL = 70
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# the group evaluation kernel for (workload, form, lbits): the roofline's
-# "traffic". C5 at lbits 6: one ncu capture of the same kernel on the same
-# law at 2,097,152 particles (lbits 5, 64 particles per leaf as at full size;
-# 309.85 MB, cold cache), scaled by the particle count (x8).
-NCU_EVAL_DRAM_BYTES: dict = {("c5", "plain", 6): 309.852160e6 * 8}
+# the kernels the roofline times for (workload, form, lbits): its "traffic".
+# C5 at lbits 6: one ncu capture of each of the same kernels on the same law
+# at 2,097,152 particles (lbits 5, 64 particles per leaf as at full size;
+# cold cache): the evaluation 228.44 MB and the far-node sums 51.15 MB,
+# scaled by the particle count (x8).
+NCU_EVAL_DRAM_BYTES: dict = {("c5", "plain", 6): (228.444672e6 + 51.145472e6) * 8}
 
 
 def parse(argv=None):
